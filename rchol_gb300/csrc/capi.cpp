@@ -1,0 +1,282 @@
+// C ABI of include/rchol_gpu.h.  Every entry point converts exceptions into
+// a status code and a thread-local message.
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "common.hpp"
+#include "host.hpp"
+
+namespace rchol {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
+void trsv(const rchol_factor_s &F, bool upper, const double *in, double *out, int k, cudaStream_t s);
+void precond(const rchol_factor_s &F, const double *r, double *z, int k, cudaStream_t s);
+void spmv_public(const rchol_matrix_s &A, const double *x, double *y, int k, cudaStream_t s);
+void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x, int k,
+                double tol, int maxit, double *relres, int *itr, cudaStream_t s);
+int64_t plan_levels(const rchol_factor_s &F, bool upper);
+
+}  // namespace rchol
+
+using namespace rchol;
+
+#define API_BEGIN try {
+#define API_END                          \
+  return RCHOL_OK;                       \
+  }                                      \
+  catch (const Error &e) {               \
+    set_last_error(e.what());            \
+    return e.status;                     \
+  }                                      \
+  catch (const std::bad_alloc &) {       \
+    set_last_error("host allocation failed"); \
+    return RCHOL_ERR_NOMEM;              \
+  }                                      \
+  catch (const std::exception &e) {      \
+    set_last_error(e.what());            \
+    return RCHOL_ERR_INTERNAL;           \
+  }
+
+static cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+extern "C" {
+
+const char *rchol_gpu_last_error(void) { return g_last_error.c_str(); }
+const char *rchol_gpu_version(void) { return "rchol_gb300 0.1 (sm_103a)"; }
+
+// ---- ordering ---------------------------------------------------------------
+
+int rchol_gpu_tree_build(int64_t n, const int64_t *row_ptr, const int64_t *col_idx, int threads,
+                         rchol_tree_t *out) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(out, "null output handle");
+  *out = nullptr;
+  *out = build_tree(n, row_ptr, col_idx, threads);
+  API_END
+}
+
+int rchol_gpu_tree_from_partition(int64_t n, const int64_t *perm, const int64_t *part,
+                                  int64_t nparts, rchol_tree_t *out) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(out, "null output handle");
+  *out = nullptr;
+  *out = tree_from_partition(n, perm, part, nparts);
+  API_END
+}
+
+int64_t rchol_gpu_tree_size(rchol_tree_t t) { return t ? t->n : -1; }
+int64_t rchol_gpu_tree_num_parts(rchol_tree_t t) { return t ? (int64_t)t->part.size() : -1; }
+
+int rchol_gpu_tree_get(rchol_tree_t t, int64_t *perm, int64_t *part) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(t, "null tree");
+  if (perm) std::memcpy(perm, t->perm.data(), t->perm.size() * sizeof(int64_t));
+  if (part) std::memcpy(part, t->part.data(), t->part.size() * sizeof(int64_t));
+  API_END
+}
+
+void rchol_gpu_tree_destroy(rchol_tree_t t) { delete t; }
+
+// ---- matrices ---------------------------------------------------------------
+
+int rchol_gpu_matrix_create(int64_t n, const int64_t *row_ptr, const int64_t *col_idx,
+                            const double *val, rchol_tree_t tree, rchol_matrix_t *out) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(out && val, "null argument");
+  *out = nullptr;
+  validate_csr(n, row_ptr, col_idx);
+  RCHOL_CHECK_ARG(!tree || tree->n == n, "tree and matrix sizes differ");
+  std::unique_ptr<rchol_matrix_s> A(new rchol_matrix_s());
+  A->n = n;
+  A->nnz = row_ptr[n];
+  if (tree) {
+    A->permuted = true;
+    A->perm = tree->perm;
+    A->host = reorder(n, row_ptr, col_idx, val, tree->perm, &A->srcpos);
+  } else {
+    A->host.n = n;
+    A->host.rp.assign(row_ptr, row_ptr + n + 1);
+    A->host.ci.assign(col_idx, col_idx + A->nnz);
+    A->host.v.assign(val, val + A->nnz);
+  }
+  std::vector<int32_t> ci32(A->nnz);
+  parallel_for(A->nnz, [&](int64_t a, int64_t b) {
+    for (int64_t i = a; i < b; ++i) ci32[i] = (int32_t)A->host.ci[i];
+  }, 1 << 20);
+  A->rp.upload(A->host.rp.data(), n + 1);
+  A->ci.upload(ci32.data(), A->nnz);
+  A->v.upload(A->host.v.data(), A->nnz);
+  RCHOL_CUDA(cudaDeviceSynchronize());
+  *out = A.release();
+  API_END
+}
+
+int64_t rchol_gpu_matrix_size(rchol_matrix_t A) { return A ? A->n : -1; }
+int64_t rchol_gpu_matrix_nnz(rchol_matrix_t A) { return A ? A->nnz : -1; }
+
+int rchol_gpu_matrix_set_values(rchol_matrix_t A, const double *val) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(A && val, "null argument");
+  if (A->permuted) {
+    for (int64_t q = 0; q < A->nnz; ++q) A->host.v[q] = val[A->srcpos[q]];
+  } else {
+    A->host.v.assign(val, val + A->nnz);
+  }
+  A->v.upload(A->host.v.data(), A->nnz);
+  RCHOL_CUDA(cudaDeviceSynchronize());
+  API_END
+}
+
+void rchol_gpu_matrix_destroy(rchol_matrix_t A) { delete A; }
+
+// ---- factorization -------------------------------------------------------------
+
+int rchol_gpu_factor(rchol_matrix_t A, rchol_tree_t tree, uint64_t seed, int precision,
+                     rchol_factor_t *out) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(A && out, "null argument");
+  *out = nullptr;
+  RCHOL_CHECK_ARG(precision == RCHOL_PREC_FP64 || precision == RCHOL_PREC_FP32, "bad precision");
+  RCHOL_CHECK_ARG(!tree || tree->n == A->n, "tree and matrix sizes differ");
+  RCHOL_CHECK_ARG(!tree || A->permuted, "matrix was created without the tree");
+  RCHOL_CHECK_ARG(tree || !A->permuted, "matrix was created with a tree; pass it");
+  HostCsr ext = extend_laplacian(A->host);
+  std::unique_ptr<rchol_factor_s> F(new rchol_factor_s());
+  F->precision = precision;
+  F->nodes = tree ? tree->nodes : trivial_nodes(A->n);
+  cudaStream_t s = 0;
+  gpu_factor(ext, F->nodes, seed, *F, s);
+  finish_factor(*F, s);
+  *out = F.release();
+  API_END
+}
+
+int rchol_gpu_factor_from_host(int64_t n, const int64_t *row_ptr, const int64_t *col_idx,
+                               const double *val, rchol_tree_t tree, int precision,
+                               rchol_factor_t *out) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(out && val, "null argument");
+  *out = nullptr;
+  RCHOL_CHECK_ARG(precision == RCHOL_PREC_FP64 || precision == RCHOL_PREC_FP32, "bad precision");
+  validate_csr(n, row_ptr, col_idx);
+  for (int64_t i = 0; i < n; ++i)
+    RCHOL_CHECK_ARG(row_ptr[i + 1] > row_ptr[i] && col_idx[row_ptr[i]] == i && val[row_ptr[i]] != 0.0,
+                    "G^T must be upper triangular with a nonzero diagonal first in every row");
+  RCHOL_CHECK_ARG(!tree || tree->n == n, "tree and factor sizes differ");
+  std::unique_ptr<rchol_factor_s> F(new rchol_factor_s());
+  F->n = n;
+  F->nnz = row_ptr[n];
+  F->precision = precision;
+  F->nodes = tree ? tree->nodes : trivial_nodes(n);
+  std::vector<int32_t> ci32(F->nnz);
+  for (int64_t i = 0; i < F->nnz; ++i) ci32[i] = (int32_t)col_idx[i];
+  cudaStream_t s = 0;
+  F->urp.upload(row_ptr, n + 1, s);
+  F->uci.upload(ci32.data(), F->nnz, s);
+  F->uv.upload(val, F->nnz, s);
+  RCHOL_CUDA(cudaStreamSynchronize(s));
+  finish_factor(*F, s);
+  *out = F.release();
+  API_END
+}
+
+int64_t rchol_gpu_factor_nnz(rchol_factor_t G) { return G ? G->nnz : -1; }
+int rchol_gpu_factor_precision(rchol_factor_t G) { return G ? G->precision : -1; }
+
+int rchol_gpu_factor_export(rchol_factor_t G, int64_t *row_ptr, int64_t *col_idx, double *val) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(G, "null factor");
+  if (row_ptr) G->urp.download(row_ptr, G->n + 1);
+  if (val) G->uv.download(val, G->nnz);
+  if (col_idx) {
+    std::vector<int32_t> ci(G->nnz);
+    G->uci.download(ci.data(), G->nnz);
+    RCHOL_CUDA(cudaDeviceSynchronize());
+    for (int64_t i = 0; i < G->nnz; ++i) col_idx[i] = ci[i];
+  }
+  RCHOL_CUDA(cudaDeviceSynchronize());
+  API_END
+}
+
+int rchol_gpu_factor_pivots(rchol_factor_t G, double *d) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(G && d, "null argument");
+  RCHOL_CHECK_ARG(G->pivots.n == (size_t)G->n, "factor has no pivots (loaded from host)");
+  G->pivots.download(d, G->n);
+  RCHOL_CUDA(cudaDeviceSynchronize());
+  API_END
+}
+
+int rchol_gpu_factor_levels(rchol_factor_t G, int64_t *fwd, int64_t *bwd) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(G && G->plan, "null factor");
+  if (fwd) *fwd = plan_levels(*G, false);
+  if (bwd) *bwd = plan_levels(*G, true);
+  API_END
+}
+
+void rchol_gpu_factor_destroy(rchol_factor_t G) { delete G; }
+
+// ---- solves -------------------------------------------------------------------------
+
+int rchol_gpu_pcg_d(rchol_matrix_t A, rchol_factor_t G, const double *d_b, double *d_x,
+                    int64_t nrhs, double tol, int maxit, double *relres, int *itr, void *stream) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(A && G && d_b && d_x && relres && itr, "null argument");
+  RCHOL_CHECK_ARG(A->n == G->n, "matrix and factor sizes differ");
+  RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
+  RCHOL_CHECK_ARG(maxit >= 0, "maxit must be nonnegative");
+  pcg_device(*A, *G, d_b, d_x, (int)nrhs, tol, maxit, relres, itr, as_stream(stream));
+  API_END
+}
+
+int rchol_gpu_pcg(rchol_matrix_t A, rchol_factor_t G, const double *b, double *x, int64_t nrhs,
+                  double tol, int maxit, double *relres, int *itr) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(A && G && b && x && relres && itr, "null argument");
+  RCHOL_CHECK_ARG(A->n == G->n, "matrix and factor sizes differ");
+  RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
+  const int64_t nk = A->n * nrhs;
+  DevBuf<double> db(nk), dx(nk);
+  db.upload(b, nk);
+  pcg_device(*A, *G, db.p, dx.p, (int)nrhs, tol, maxit, relres, itr, 0);
+  dx.download(x, nk);
+  RCHOL_CUDA(cudaDeviceSynchronize());
+  API_END
+}
+
+int rchol_gpu_precond_d(rchol_factor_t G, const double *d_r, double *d_z, int64_t nrhs,
+                        void *stream) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(G && d_r && d_z, "null argument");
+  RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
+  precond(*G, d_r, d_z, (int)nrhs, as_stream(stream));
+  API_END
+}
+
+int rchol_gpu_trsv_d(rchol_factor_t G, int transpose, const double *d_in, double *d_out,
+                     int64_t nrhs, void *stream) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(G && d_in && d_out, "null argument");
+  RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
+  trsv(*G, transpose != 0, d_in, d_out, (int)nrhs, as_stream(stream));
+  API_END
+}
+
+int rchol_gpu_spmv_d(rchol_matrix_t A, const double *d_x, double *d_y, int64_t nrhs, void *stream) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(A && d_x && d_y, "null argument");
+  RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
+  spmv_public(*A, d_x, d_y, (int)nrhs, as_stream(stream));
+  API_END
+}
+
+}  // extern "C"

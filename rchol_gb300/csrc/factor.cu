@@ -1,0 +1,475 @@
+// Randomized Cholesky factorization of the extended Laplacian on the GPU.
+//
+// Replaces c++/rchol_lap/rchol_lap.cpp: process_array (:778-855),
+// recursive_calculation (:187-355), linear_update (:733-770),
+// random_sampling0 (:643-729) and coalesce (:358-387).
+//
+// Schedule.  The nested-dissection tree is processed one depth at a time,
+// leaves first.  One warp owns one tree node and eliminates its columns in
+// order; nodes of the same depth are independent (a fill edge never joins two
+// sibling subtrees), so a launch covers every node of a depth.
+//
+// Column store.  Every column c owns a slab of fill records {row, source, w}
+// in HBM (capacity fcap[c]).  Eliminating column j appends each sampled edge
+// to the slab of its smaller endpoint with one atomicAdd on that column's
+// counter -- the same store serves node-internal fill (the reference's
+// gsl_spmatrix_set) and fill deferred to an ancestor separator (its sep_edge
+// lists).  A slab that would overflow sets a flag; the host then enlarges the
+// slabs that overflowed and runs the factorization again, which gives the
+// same result because nothing depends on timing.
+//
+// Per column (one warp, shared memory only):
+//   1. gather the initial entries (CSR row c of the upper extended Laplacian,
+//      minus the diagonal and negative ground edges) and the fill records;
+//   2. rank-sort by (row, source) and sum duplicate rows left to right;
+//   3. rank-sort by (weight, row), warp Hillis-Steele prefix sum;
+//   4. sample the m-1 fill edges in parallel, one lane per edge, with a
+//      Philox4x32-10 uniform keyed by (seed, c, i) and a binary search;
+//   5. write the column of G: sqrt(d) then -(w/d)*sqrt(d) per row.
+// All rounding is explicit (_rn intrinsics), so the result equals the
+// device-contract mode of the CPU restatement bit for bit.
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "common.hpp"
+#include "host.hpp"
+
+namespace rchol {
+
+namespace {
+
+struct FillRec {
+  uint32_t row;
+  uint32_t src;  // eliminated column + 1
+  double w;
+};
+static_assert(sizeof(FillRec) == 16, "FillRec layout");
+
+enum { FLAG_FILL = 0, FLAG_WIDTH = 1, FLAG_GCAP = 2, FLAG_SINGULAR = 3, NFLAGS = 4 };
+
+struct ElimArgs {
+  const int64_t *lrp;  // extended Laplacian, upper CSR
+  const int32_t *lci;
+  const double *lv;
+  int64_t next;        // n + 1 (ground vertex = next - 1)
+  const int64_t *node_begin;
+  const int64_t *node_end;
+  int num_nodes;
+  uint32_t *fcnt;
+  const uint32_t *fcap;
+  const int64_t *fbase;
+  FillRec *frec;
+  int64_t *gstart;
+  uint32_t *gcnt;
+  int32_t *grow;
+  double *gval;
+  unsigned long long *gtop;
+  int64_t gcap;
+  double *diag;
+  int *flags;
+  uint64_t seed;
+  int emax;  // per-warp shared-memory capacity in entries
+};
+
+__device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b) { return __umulhi(a, b); }
+
+// Philox4x32-10 (Salmon et al., SC'11).
+__device__ __forceinline__ void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    uint32_t hi0 = mulhi32(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    uint32_t hi1 = mulhi32(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+    uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+  }
+}
+
+__device__ __forceinline__ double uniform53(uint64_t seed, uint64_t v, uint32_t i) {
+  uint32_t c[4] = {i >> 1, 0u, (uint32_t)v, (uint32_t)(v >> 32)};
+  philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  uint32_t a = (i & 1) ? c[2] : c[0];
+  uint32_t b = (i & 1) ? c[3] : c[1];
+  return __dmul_rn(__dadd_rn(__dmul_rn((double)(a >> 5), 67108864.0), (double)(b >> 6)),
+                   1.0 / 9007199254740992.0);
+}
+
+__device__ __forceinline__ bool wless(double wa, uint32_t ra, double wb, uint32_t rb) {
+  return wa < wb || (wa == wb && ra < rb);
+}
+
+__global__ void eliminate_kernel(ElimArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int warp = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (warp >= a.num_nodes) return;
+  const int E = a.emax;
+  // per-warp layout: akey[E] aval[E] bkey[E] bval[E] cs[E]
+  unsigned char *base = smem_raw + (size_t)wib * (size_t)E * 40;
+  uint64_t *akey = reinterpret_cast<uint64_t *>(base);
+  double *aval = reinterpret_cast<double *>(base + (size_t)E * 8);
+  uint64_t *bkey = reinterpret_cast<uint64_t *>(base + (size_t)E * 16);
+  double *bval = reinterpret_cast<double *>(base + (size_t)E * 24);
+  double *cs = reinterpret_cast<double *>(base + (size_t)E * 32);
+
+  const int64_t ground = a.next - 1;
+  const int64_t cb = a.node_begin[warp], ce = a.node_end[warp];
+  for (int64_t c = cb; c < ce; ++c) {
+    // ---- 1. gather ----------------------------------------------------------
+    const int64_t r0 = a.lrp[c], r1 = a.lrp[c + 1];
+    uint32_t nfill = __ldcg(&a.fcnt[c]);
+    const uint32_t cap = a.fcap[c];
+    if (nfill > cap) nfill = cap;  // overflow already flagged by the writer
+    int ninit = 0;
+    // initial entries: count kept ones with a ballot per 32-wide chunk
+    for (int64_t k0 = r0; k0 < r1; k0 += 32) {
+      int64_t k = k0 + lane;
+      bool keep = false;
+      int32_t col = 0;
+      double v = 0.0;
+      if (k < r1) {
+        col = a.lci[k];
+        v = a.lv[k];
+        keep = (col != c) && !(col == ground && v < 0.0 && c != ground);
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, keep);
+      int pos = ninit + __popc(bal & ((1u << lane) - 1u));
+      if (keep && pos < E) {
+        akey[pos] = ((uint64_t)(uint32_t)col << 32);
+        aval[pos] = v;
+      }
+      ninit += __popc(bal);
+    }
+    const int64_t fb = a.fbase[c];
+    int total = ninit + (int)nfill;
+    if (total > E) {
+      if (lane == 0) atomicMax(&a.flags[FLAG_WIDTH], total);
+      total = 0;  // skip the column; the host retries with wider buffers
+    }
+    for (uint32_t f = lane; f < nfill && total; f += 32) {
+      const FillRec *rp = &a.frec[fb + f];
+      uint32_t row = __ldcg(&rp->row), src = __ldcg(&rp->src);
+      double w = __ldcg(&rp->w);
+      akey[ninit + f] = ((uint64_t)row << 32) | src;
+      aval[ninit + f] = w;
+    }
+    __syncwarp();
+    // ---- 2. sort by (row, source) and merge --------------------------------
+    for (int e = lane; e < total; e += 32) {
+      uint64_t ke = akey[e];
+      int rank = 0;
+      for (int f = 0; f < total; ++f) rank += (akey[f] < ke);
+      bkey[rank] = ke;
+      bval[rank] = aval[e];
+    }
+    __syncwarp();
+    int m = 0;
+    for (int e0 = 0; e0 < total; e0 += 32) {
+      int e = e0 + lane;
+      bool head = false;
+      uint32_t row = 0;
+      if (e < total) {
+        row = (uint32_t)(bkey[e] >> 32);
+        head = (e == 0) || ((uint32_t)(bkey[e - 1] >> 32) != row);
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, head);
+      int pos = m + __popc(bal & ((1u << lane) - 1u));
+      if (head) {
+        double s = bval[e];
+        for (int f = e + 1; f < total && (uint32_t)(bkey[f] >> 32) == row; ++f) s = __dadd_rn(s, bval[f]);
+        akey[pos] = row;  // rows ascending
+        aval[pos] = s;
+      }
+      m += __popc(bal);
+    }
+    __syncwarp();
+    // ---- 3. sort by (weight, row), prefix sum --------------------------------
+    for (int e = lane; e < m; e += 32) {
+      double we = aval[e];
+      uint32_t re = (uint32_t)akey[e];
+      int rank = 0;
+      for (int f = 0; f < m; ++f) rank += wless(aval[f], (uint32_t)akey[f], we, re);
+      bkey[rank] = re;
+      bval[rank] = we;
+    }
+    __syncwarp();
+    double carry = 0.0;
+    for (int e0 = 0; e0 < m; e0 += 32) {
+      int e = e0 + lane;
+      double v = (e < m) ? bval[e] : 0.0;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        double t = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v = __dadd_rn(t, v);
+      }
+      double out = __dadd_rn(carry, v);
+      if (e < m) cs[e] = out;
+      int last = min(31, m - 1 - e0);
+      carry = __shfl_sync(0xffffffffu, out, last);
+    }
+    __syncwarp();
+    const double csum = m ? cs[m - 1] : 0.0;
+    // ---- 4. sample ----------------------------------------------------------
+    for (int i = lane; i < m - 1; i += 32) {
+      double u = uniform53(a.seed, (uint64_t)c, (uint32_t)i);
+      double tar = cs[i];
+      double span = __dsub_rn(csum, tar);
+      double r = __dadd_rn(__dmul_rn(u, span), tar);
+      int lo = i, hi = m;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (cs[mid] < r) lo = mid + 1;
+        else hi = mid;
+      }
+      int k = lo < m ? lo : m - 1;
+      if (k == i) continue;
+      double wn = __ddiv_rn(__dmul_rn(bval[i], span), csum);
+      uint32_t ri = (uint32_t)bkey[i], rk = (uint32_t)bkey[k];
+      uint32_t t = min(ri, rk), mx = max(ri, rk);
+      uint32_t slot = atomicAdd(&a.fcnt[t], 1u);
+      if (slot < a.fcap[t]) {
+        FillRec rec;
+        rec.row = mx;
+        rec.src = (uint32_t)c + 1u;
+        rec.w = wn;
+        a.frec[a.fbase[t] + slot] = rec;
+      } else {
+        atomicOr(&a.flags[FLAG_FILL], 1);
+      }
+    }
+    // ---- 5. column of G -------------------------------------------------------
+    if (c != ground) {
+      bool hasg = (m > 0) && ((int64_t)(uint32_t)akey[m - 1] == ground);
+      int cnt = 1 + m - (hasg ? 1 : 0);
+      unsigned long long gs = 0;
+      if (lane == 0) {
+        gs = atomicAdd(a.gtop, (unsigned long long)cnt);
+        a.diag[c] = csum;
+        if (!(csum > 0.0)) atomicOr(&a.flags[FLAG_SINGULAR], 1);
+      }
+      gs = __shfl_sync(0xffffffffu, gs, 0);
+      if ((int64_t)(gs + cnt) > a.gcap) {
+        if (lane == 0) atomicOr(&a.flags[FLAG_GCAP], 1);
+      } else {
+        double sq = __dsqrt_rn(csum);
+        double inv = __ddiv_rn(1.0, csum);
+        if (lane == 0) {
+          a.gstart[c] = (int64_t)gs;
+          a.gcnt[c] = (uint32_t)cnt;
+          a.grow[gs] = (int32_t)c;
+          a.gval[gs] = sq;
+        }
+        for (int e = lane; e < cnt - 1; e += 32) {
+          a.grow[gs + 1 + e] = (int32_t)(uint32_t)akey[e];
+          a.gval[gs + 1 + e] = __dmul_rn(-__dmul_rn(aval[e], inv), sq);
+        }
+      }
+    } else if (lane == 0) {
+      a.diag[c] = csum;
+    }
+    __syncwarp();
+  }
+}
+
+// ---- CSR assembly ----------------------------------------------------------
+
+__global__ void copy_columns_kernel(int64_t n, const int64_t *gstart, const uint32_t *gcnt,
+                                    const int32_t *grow, const double *gval, const int64_t *urp,
+                                    int32_t *uci, double *uv) {
+  int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  int64_t s = gstart[warp], o = urp[warp];
+  uint32_t c = gcnt[warp];
+  for (uint32_t e = lane; e < c; e += 32) {
+    uci[o + e] = grow[s + e];
+    uv[o + e] = gval[s + e];
+  }
+}
+
+__global__ void u32_to_i64_kernel(int64_t n, const uint32_t *a, int64_t *b) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+
+}  // namespace
+
+// Exclusive scan of int64 counts in place: out[0..n] with out[n] = total.
+void exclusive_scan_i64(int64_t *d_data, int64_t n, cudaStream_t s);
+
+namespace {
+
+int pow2_at_least(int x) {
+  int p = 32;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+}  // namespace
+
+void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t seed,
+                rchol_factor_s &F, cudaStream_t s) {
+  const int64_t next = ext.n, n = next - 1;
+  RCHOL_CHECK_ARG(next < (int64_t)UINT32_MAX - 1, "matrix too large for 32-bit vertex ids");
+  // device copy of the extended Laplacian (int32 column indices)
+  DevBuf<int64_t> lrp;
+  DevBuf<int32_t> lci;
+  DevBuf<double> lv;
+  {
+    std::vector<int32_t> ci32(ext.ci.size());
+    parallel_for((int64_t)ext.ci.size(), [&](int64_t a0, int64_t b0) {
+      for (int64_t i = a0; i < b0; ++i) ci32[i] = (int32_t)ext.ci[i];
+    }, 1 << 20);
+    lrp.upload(ext.rp.data(), ext.rp.size(), s);
+    lci.upload(ci32.data(), ci32.size(), s);
+    lv.upload(ext.v.data(), ext.v.size(), s);
+    RCHOL_CUDA(cudaStreamSynchronize(s));
+  }
+  // depth of every column and node lists per depth
+  int maxdepth = 1;
+  for (auto &nd : nodes) maxdepth = std::max(maxdepth, nd.depth);
+  std::vector<int> coldepth(next, 1);
+  std::vector<char> colleaf(next, 0);
+  for (auto &nd : nodes)
+    for (int64_t c = nd.begin; c < nd.end; ++c) {
+      coldepth[c] = nd.depth;
+      colleaf[c] = nd.leaf;
+    }
+  std::vector<int> initdeg(next);
+  for (int64_t c = 0; c < next; ++c) initdeg[c] = (int)(ext.rp[c + 1] - ext.rp[c]);
+  // initial slab capacities: small for leaf columns, larger for separators
+  std::vector<uint32_t> cap(next);
+  for (int64_t c = 0; c < next; ++c) cap[c] = colleaf[c] ? 48u : 192u;
+  int64_t gcap = std::max<int64_t>(ext.nnz() * 10, 1024);
+
+  cudaDeviceProp prop;
+  int dev;
+  RCHOL_CUDA(cudaGetDevice(&dev));
+  RCHOL_CUDA(cudaGetDeviceProperties(&prop, dev));
+  const size_t smem_limit = prop.sharedMemPerBlockOptin;
+  RCHOL_CUDA(cudaFuncSetAttribute(eliminate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem_limit));
+
+  DevBuf<double> diag(next);
+  DevBuf<int> flags(NFLAGS);
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    std::vector<int64_t> base(next + 1, 0);
+    for (int64_t c = 0; c < next; ++c) base[c + 1] = base[c] + cap[c];
+    DevBuf<uint32_t> fcnt(next), fcap(next);
+    DevBuf<int64_t> fbase(next);
+    DevBuf<FillRec> frec(std::max<int64_t>(base[next], 1));
+    DevBuf<int64_t> gstart(next);
+    DevBuf<uint32_t> gcnt(next);
+    DevBuf<int32_t> grow(gcap);
+    DevBuf<double> gval(gcap);
+    DevBuf<unsigned long long> gtop(1);
+    RCHOL_CUDA(cudaMemsetAsync(fcnt.p, 0, fcnt.bytes(), s));
+    RCHOL_CUDA(cudaMemsetAsync(gcnt.p, 0, gcnt.bytes(), s));
+    RCHOL_CUDA(cudaMemsetAsync(gstart.p, 0, gstart.bytes(), s));
+    RCHOL_CUDA(cudaMemsetAsync(gtop.p, 0, gtop.bytes(), s));
+    RCHOL_CUDA(cudaMemsetAsync(flags.p, 0, flags.bytes(), s));
+    fcap.upload(cap.data(), next, s);
+    fbase.upload(base.data(), next, s);
+
+    ElimArgs args;
+    args.lrp = lrp.p;
+    args.lci = lci.p;
+    args.lv = lv.p;
+    args.next = next;
+    args.fcnt = fcnt.p;
+    args.fcap = fcap.p;
+    args.fbase = fbase.p;
+    args.frec = frec.p;
+    args.gstart = gstart.p;
+    args.gcnt = gcnt.p;
+    args.grow = grow.p;
+    args.gval = gval.p;
+    args.gtop = gtop.p;
+    args.gcap = gcap;
+    args.diag = diag.p;
+    args.flags = flags.p;
+    args.seed = seed;
+    std::vector<DevBuf<int64_t>> keep;
+    for (int depth = maxdepth; depth >= 1; --depth) {
+      std::vector<int64_t> nb, ne;
+      int width = 32;
+      for (auto &nd : nodes) {
+        if (nd.depth != depth || nd.end <= nd.begin) continue;
+        nb.push_back(nd.begin);
+        ne.push_back(nd.end);
+        for (int64_t c = nd.begin; c < nd.end; ++c)
+          width = std::max(width, initdeg[c] + (int)cap[c]);
+      }
+      if (nb.empty()) continue;
+      int emax = pow2_at_least(width);
+      size_t per_warp = (size_t)emax * 40;
+      RCHOL_CHECK_ARG(per_warp <= smem_limit, "column too wide for shared memory");
+      int wpb = (int)std::min<size_t>(4, smem_limit / per_warp);
+      keep.emplace_back(nb.size());
+      keep.back().upload(nb.data(), nb.size(), s);
+      keep.emplace_back(ne.size());
+      keep.back().upload(ne.data(), ne.size(), s);
+      args.node_begin = keep[keep.size() - 2].p;
+      args.node_end = keep.back().p;
+      args.num_nodes = (int)nb.size();
+      args.emax = emax;
+      int blocks = (int)((nb.size() + wpb - 1) / wpb);
+      eliminate_kernel<<<blocks, wpb * 32, per_warp * wpb, s>>>(args);
+      RCHOL_CUDA(cudaGetLastError());
+    }
+    int hflags[NFLAGS];
+    flags.download(hflags, NFLAGS, s);
+    RCHOL_CUDA(cudaStreamSynchronize(s));
+    if (hflags[FLAG_FILL] || hflags[FLAG_WIDTH]) {
+      std::vector<uint32_t> cnt(next);
+      fcnt.download(cnt.data(), next, s);
+      RCHOL_CUDA(cudaStreamSynchronize(s));
+      for (int64_t c = 0; c < next; ++c)
+        if (cnt[c] >= cap[c]) cap[c] = std::max<uint32_t>(cap[c] * 2, cnt[c] + 16);
+      continue;
+    }
+    if (hflags[FLAG_GCAP]) {
+      gcap *= 2;
+      continue;
+    }
+    if (hflags[FLAG_SINGULAR])
+      throw Error(RCHOL_ERR_SINGULAR,
+                  "factorization produced a zero pivot (a connected component without "
+                  "diagonal excess: the matrix is singular)");
+    // ---- assemble U = CSR of G^T --------------------------------------------
+    F.n = n;
+    F.urp.alloc(n + 1);
+    {
+      int64_t blocks = (n + 255) / 256;
+      u32_to_i64_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, gcnt.p, F.urp.p);
+      RCHOL_CUDA(cudaGetLastError());
+      exclusive_scan_i64(F.urp.p, n, s);
+      int64_t nnz = 0;
+      RCHOL_CUDA(cudaMemcpyAsync(&nnz, F.urp.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+      RCHOL_CUDA(cudaStreamSynchronize(s));
+      F.nnz = nnz;
+      F.uci.alloc(nnz);
+      F.uv.alloc(nnz);
+      int64_t threads = n * 32;
+      copy_columns_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+          n, gstart.p, gcnt.p, grow.p, gval.p, F.urp.p, F.uci.p, F.uv.p);
+      RCHOL_CUDA(cudaGetLastError());
+    }
+    F.pivots.alloc(n);
+    RCHOL_CUDA(cudaMemcpyAsync(F.pivots.p, diag.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    RCHOL_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+  throw Error(RCHOL_ERR_INTERNAL, "factorization buffers did not converge");
+}
+
+}  // namespace rchol

@@ -1,0 +1,767 @@
+// Triangular solves with G, SpMV with A and the PCG loop of
+// c++/util/pcg.cpp:57-159 on the GPU.
+//
+// Triangular solves.  G comes from a nested-dissection elimination, so row i
+// of G only references columns in i's own tree node or in its descendants.
+// The forward solve y = G^-1 r walks the tree from the leaves to the root, the
+// backward solve z = G^-T y from the root to the leaves; all nodes of one depth
+// are independent and go in one launch, one thread block per node.  Inside a
+// node the block
+//   A. streams every row's entries that point outside the node (already
+//      solved) and forms the partial right-hand side (bandwidth bound);
+//   B. solves the node's own triangular block level by level (rows of a level
+//      are independent), keeping the node's unknowns in shared memory;
+//   C. writes the node's unknowns out.
+// Levels, the row split between A and B, and 1/G_ii are precomputed per
+// factor (SolvePlan).  Values are FP64 or, for an FP32 factor, FP32 with FP32
+// accumulation ("applied in FP32"); the right-hand side comes in as FP64 and
+// the result leaves as FP64.
+//
+// Several right-hand sides are stored row-major (n x k) and solved in one
+// traversal: lanes then run over the right-hand sides of a row.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "common.hpp"
+#include "host.hpp"
+
+namespace rchol {
+
+void exclusive_scan_i64(int64_t *d_data, int64_t n, cudaStream_t s);
+
+struct DirPlan {
+  std::vector<int> stage_ptr;   // nodes of stage s: [stage_ptr[s], stage_ptr[s+1])
+  std::vector<int> stage_maxrows;
+  DevBuf<int64_t> nb, ne;       // node row range (clipped to n)
+  DevBuf<int64_t> lvl_off;      // node k owns level entries [lvl_off[k], lvl_off[k+1])
+  DevBuf<int64_t> level_ptr;    // row offsets of each level (size = total levels + 1 per node, packed)
+  DevBuf<int32_t> rows;         // rows in per-node level order
+  DevBuf<int32_t> split;        // fwd: #leading external entries; bwd: index of first trailing external entry
+  int64_t crit_levels = 0;      // sum over stages of the deepest node
+};
+
+struct SolvePlan {
+  DirPlan fwd, bwd;
+  DevBuf<double> dinv;
+  DevBuf<float> dinv32;
+  int64_t dag_fwd = 0, dag_bwd = 0;
+  DevBuf<double> scratch;  // global fallback for nodes too large for shared memory
+  DevBuf<float> scratch32;
+  DevBuf<double> ytmp;     // intermediate of precond (FP64 path)
+  DevBuf<float> ytmp32;    // intermediate of precond (FP32 path)
+};
+
+void destroy_plan(SolvePlan *p) { delete p; }
+
+namespace {
+
+constexpr int TRSV_THREADS = 256;
+constexpr size_t TRSV_SMEM = 96 * 1024;
+
+template <typename VT>
+struct TrsvArgs {
+  const int64_t *rp;
+  const int32_t *ci;
+  const VT *val;
+  const VT *dinv;
+  const int64_t *nb, *ne, *lvl_off, *level_ptr;
+  const int32_t *rows, *split;
+  int node0;
+  int k;
+  bool upper;  // false: forward with L (external = leading), true: backward with U (trailing)
+  int64_t smem_rows;
+  VT *scratch;
+};
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename VT, typename InT, typename OutT>
+__global__ void __launch_bounds__(TRSV_THREADS) trsv_stage_kernel(TrsvArgs<VT> a, const InT *in, OutT *out) {
+  extern __shared__ unsigned char smem_raw[];
+  const int node = a.node0 + blockIdx.x;
+  const int64_t b = a.nb[node], e = a.ne[node];
+  const int64_t size = e - b;
+  if (size <= 0) return;
+  const int k = a.k;
+  VT *xs = (size <= a.smem_rows) ? reinterpret_cast<VT *>(smem_raw) : a.scratch + b * k;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+
+  // ---- A: right-hand side minus the external part ----------------------------
+  for (int64_t i = b + warp; i < e; i += nw) {
+    const int64_t r0 = a.rp[i], r1 = a.rp[i + 1];
+    int64_t x0, x1;  // external entry range
+    if (!a.upper) {
+      x0 = r0;
+      x1 = r0 + a.split[i];
+    } else {
+      x0 = r0 + a.split[i];
+      x1 = r1;
+    }
+    if (k == 1) {
+      VT s = 0;
+      for (int64_t q = x0 + lane; q < x1; q += 32) s += a.val[q] * (VT)out[a.ci[q]];
+      s = warp_sum(s);
+      if (lane == 0) xs[i - b] = (VT)in[i] - s;
+    } else {
+      for (int r = lane; r < k; r += 32) {
+        VT s = 0;
+        for (int64_t q = x0; q < x1; ++q) s += a.val[q] * (VT)out[(int64_t)a.ci[q] * k + r];
+        xs[(i - b) * k + r] = (VT)in[i * k + r] - s;
+      }
+    }
+  }
+  __syncthreads();
+  // ---- B: the node's own triangle, level by level ---------------------------
+  // level boundaries of this node: level_ptr[l0 .. l1] (the last one is the end)
+  const int64_t l0 = a.lvl_off[node], l1 = a.lvl_off[node + 1] - 1;
+  for (int64_t lv = l0; lv < l1; ++lv) {
+    const int64_t p0 = a.level_ptr[lv], p1 = a.level_ptr[lv + 1];
+    for (int64_t p = p0 + warp; p < p1; p += nw) {
+      const int64_t i = a.rows[p];
+      const int64_t r0 = a.rp[i], r1 = a.rp[i + 1];
+      int64_t q0, q1;  // internal off-diagonal entries
+      if (!a.upper) {
+        q0 = r0 + a.split[i];
+        q1 = r1 - 1;  // the diagonal is last
+      } else {
+        q0 = r0 + 1;  // the diagonal is first
+        q1 = r0 + a.split[i];
+      }
+      if (k == 1) {
+        VT s = 0;
+        for (int64_t q = q0 + lane; q < q1; q += 32) s += a.val[q] * xs[a.ci[q] - b];
+        s = warp_sum(s);
+        if (lane == 0) xs[i - b] = (xs[i - b] - s) * a.dinv[i];
+      } else {
+        for (int r = lane; r < k; r += 32) {
+          VT s = 0;
+          for (int64_t q = q0; q < q1; ++q) s += a.val[q] * xs[(int64_t)(a.ci[q] - b) * k + r];
+          xs[(i - b) * k + r] = (xs[(i - b) * k + r] - s) * a.dinv[i];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // ---- C: write the node's unknowns -------------------------------------------
+  for (int64_t t = threadIdx.x; t < size * k; t += blockDim.x) out[b * k + t] = (OutT)xs[t];
+}
+
+template <typename VT, typename InT, typename OutT>
+void run_trsv(const rchol_factor_s &F, const SolvePlan &P, bool upper, const InT *in, OutT *out,
+              int k, cudaStream_t s) {
+  const DirPlan &D = upper ? P.bwd : P.fwd;
+  TrsvArgs<VT> a;
+  if (!upper) {
+    a.rp = F.lrp.p;
+    a.ci = F.lci.p;
+  } else {
+    a.rp = F.urp.p;
+    a.ci = F.uci.p;
+  }
+  if constexpr (sizeof(VT) == 8) {
+    a.val = reinterpret_cast<const VT *>(upper ? F.uv.p : F.lv.p);
+    a.dinv = reinterpret_cast<const VT *>(P.dinv.p);
+    a.scratch = reinterpret_cast<VT *>(P.scratch.p);
+  } else {
+    a.val = reinterpret_cast<const VT *>(upper ? F.uv32.p : F.lv32.p);
+    a.dinv = reinterpret_cast<const VT *>(P.dinv32.p);
+    a.scratch = reinterpret_cast<VT *>(P.scratch32.p);
+  }
+  a.nb = D.nb.p;
+  a.ne = D.ne.p;
+  a.lvl_off = D.lvl_off.p;
+  a.level_ptr = D.level_ptr.p;
+  a.rows = D.rows.p;
+  a.split = D.split.p;
+  a.k = k;
+  a.upper = upper;
+  a.smem_rows = (int64_t)(TRSV_SMEM / (sizeof(VT) * (size_t)k));
+  static bool attr_set = false;
+  if (!attr_set) {
+    RCHOL_CUDA(cudaFuncSetAttribute(trsv_stage_kernel<VT, InT, OutT>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRSV_SMEM));
+    attr_set = true;
+  }
+  for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
+    int nodes = D.stage_ptr[st + 1] - D.stage_ptr[st];
+    if (!nodes) continue;
+    a.node0 = D.stage_ptr[st];
+    int64_t maxrows = D.stage_maxrows[st];
+    size_t smem = (size_t)std::min<int64_t>(maxrows, a.smem_rows) * sizeof(VT) * k;
+    trsv_stage_kernel<VT, InT, OutT><<<nodes, TRSV_THREADS, smem, s>>>(a, in, out);
+    RCHOL_CUDA(cudaGetLastError());
+  }
+}
+
+// ---- SpMV ---------------------------------------------------------------------
+
+// y = A x for one right-hand side: LPR lanes per row.
+template <int LPR>
+__global__ void spmv1_kernel(int64_t n, const int64_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                             const double *__restrict__ v, const double *__restrict__ x,
+                             double *__restrict__ y) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t row = t / LPR;
+  int sub = (int)(t % LPR);
+  if (row >= n) return;
+  double s = 0.0;
+  for (int64_t q = rp[row] + sub; q < rp[row + 1]; q += LPR) s += v[q] * x[ci[q]];
+#pragma unroll
+  for (int o = LPR / 2; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
+  if (sub == 0) y[row] = s;
+}
+
+// y = A x for k right-hand sides stored row-major; one warp per row, lanes over k.
+__global__ void spmvk_kernel(int64_t n, int k, const int64_t *__restrict__ rp,
+                             const int32_t *__restrict__ ci, const double *__restrict__ v,
+                             const double *__restrict__ x, double *__restrict__ y) {
+  int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  for (int r = lane; r < k; r += 32) {
+    double s = 0.0;
+    for (int64_t q = rp[row]; q < rp[row + 1]; ++q) s += v[q] * x[(int64_t)ci[q] * k + r];
+    y[row * k + r] = s;
+  }
+}
+
+void spmv(const rchol_matrix_s &A, const double *x, double *y, int k, cudaStream_t s) {
+  const int64_t n = A.n;
+  if (k == 1) {
+    int64_t threads = n * 8;
+    spmv1_kernel<8><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, A.rp.p, A.ci.p, A.v.p, x, y);
+  } else {
+    int64_t threads = n * 32;
+    spmvk_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, k, A.rp.p, A.ci.p, A.v.p, x, y);
+  }
+  RCHOL_CUDA(cudaGetLastError());
+}
+
+// ---- PCG --------------------------------------------------------------------------
+//
+// Per right-hand side r the device keeps: bnorm2, rnorm2, rz, rz_prev, pr, pq,
+// alpha, beta, active, iters.  Every reduction is deterministic: a fixed grid,
+// a fixed per-thread assignment, fixed-shape trees.
+
+constexpr int RED_BLOCKS = 512;
+constexpr int RED_THREADS = 256;
+
+struct PcgState {
+  double *bnorm2, *rnorm2, *rz, *rz_prev, *pr, *pq, *alpha, *beta;
+  int *active, *iters;
+  int *any_active;
+  double *partial;  // RED_BLOCKS * k * 2
+  int k;
+  double tol;
+  int maxit;
+};
+
+enum RedOp { RED_DOT = 0, RED_DOT2 = 1, RED_UPDATE = 2, RED_RESID = 3 };
+
+// Generic per-RHS reduction over rows.  Thread mapping: rhs = t % k,
+// row lane = t / k with a power-of-two number of row lanes per block.
+template <int OP>
+__global__ void __launch_bounds__(RED_THREADS) reduce_kernel(int64_t n, PcgState st, const double *a,
+                                                             const double *b, double *c, double *d,
+                                                             const double *e) {
+  __shared__ double sh[2][RED_THREADS];
+  const int k = st.k;
+  if (OP != RED_RESID && !*st.any_active) return;
+  int lanes = 1;
+  while (lanes * 2 * k <= RED_THREADS) lanes *= 2;
+  const int t = threadIdx.x;
+  const int r = t % k, rl = t / k;
+  const bool act_t = (k <= RED_THREADS) && (rl < lanes);
+  int64_t per = (n + gridDim.x - 1) / gridDim.x;
+  int64_t i0 = blockIdx.x * per, i1 = min(n, i0 + per);
+  double s0 = 0.0, s1 = 0.0;
+  if (act_t) {
+    if (OP == RED_DOT) {  // s0 = a.b
+      for (int64_t i = i0 + rl; i < i1; i += lanes) s0 += a[i * k + r] * b[i * k + r];
+    } else if (OP == RED_DOT2) {  // s0 = a.b, s1 = a.e  (p.q and p.r)
+      for (int64_t i = i0 + rl; i < i1; i += lanes) {
+        double pv = a[i * k + r];
+        s0 += pv * b[i * k + r];
+        s1 += pv * e[i * k + r];
+      }
+    } else if (OP == RED_UPDATE) {  // x += alpha p ; r -= alpha q ; s0 = r.r
+      double al = st.active[r] ? st.alpha[r] : 0.0;
+      bool on = st.active[r];
+      for (int64_t i = i0 + rl; i < i1; i += lanes) {
+        int64_t o = i * k + r;
+        double rv = d[o];
+        if (on) {
+          c[o] += al * a[o];
+          rv += -al * b[o];
+          d[o] = rv;
+        }
+        s0 += rv * rv;
+      }
+    } else {  // RED_RESID: s0 = (a - b).(a - b)  with a = A x, b = rhs
+      for (int64_t i = i0 + rl; i < i1; i += lanes) {
+        double q = a[i * k + r] + -1.0 * b[i * k + r];
+        s0 += q * q;
+      }
+    }
+  }
+  sh[0][t] = s0;
+  sh[1][t] = s1;
+  __syncthreads();
+  for (int h = lanes / 2; h > 0; h >>= 1) {
+    if (act_t && rl < h) {
+      sh[0][t] += sh[0][t + h * k];
+      sh[1][t] += sh[1][t + h * k];
+    }
+    __syncthreads();
+  }
+  if (act_t && rl == 0) {
+    st.partial[(int64_t)blockIdx.x * k + r] = sh[0][t];
+    st.partial[(int64_t)(gridDim.x + blockIdx.x) * k + r] = sh[1][t];
+  }
+}
+
+// Sum the RED_BLOCKS partials of every rhs (one block per rhs, fixed tree).
+__device__ double block_total(const double *part, int k, int r, int which) {
+  __shared__ double sh[RED_THREADS];
+  double s = 0.0;
+  for (int bb = threadIdx.x; bb < RED_BLOCKS; bb += RED_THREADS)
+    s += part[(int64_t)(which * RED_BLOCKS + bb) * k + r];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = RED_THREADS / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  double tot = sh[0];
+  __syncthreads();
+  return tot;
+}
+
+enum FinOp { FIN_INIT = 0, FIN_BETA = 1, FIN_ALPHA = 2, FIN_CONV = 3, FIN_RESID = 4 };
+
+__global__ void finalize_kernel(PcgState st, int op, int first, double *relres) {
+  const int r = blockIdx.x;
+  if (op != FIN_INIT && op != FIN_RESID && !*st.any_active) return;
+  double t0 = block_total(st.partial, st.k, r, 0);
+  double t1 = block_total(st.partial, st.k, r, 1);
+  if (threadIdx.x != 0) return;
+  if (op == FIN_INIT) {  // t0 = b.b (r = b)
+    st.bnorm2[r] = t0;
+    st.rnorm2[r] = t0;
+    st.iters[r] = 0;
+    int act = (sqrt(t0) > sqrt(t0) * st.tol) && (st.maxit > 0);
+    st.active[r] = act;
+    if (act) atomicOr(st.any_active, 1);
+  } else if (op == FIN_BETA) {  // t0 = r.z
+    if (st.active[r]) {
+      st.beta[r] = first ? 0.0 : t0 / st.rz_prev[r];
+      st.rz[r] = t0;
+    }
+  } else if (op == FIN_ALPHA) {  // t0 = p.q, t1 = p.r
+    if (st.active[r]) {
+      st.pq[r] = t0;
+      st.pr[r] = t1;
+      st.alpha[r] = t1 / t0;
+    }
+  } else if (op == FIN_CONV) {  // t0 = r.r after the update
+    if (st.active[r]) {
+      st.rnorm2[r] = t0;
+      st.rz_prev[r] = st.rz[r];
+      int it = st.iters[r] + 1;
+      st.iters[r] = it;
+      st.active[r] = (sqrt(t0) > sqrt(st.bnorm2[r]) * st.tol) && (it < st.maxit);
+    }
+  } else {  // FIN_RESID
+    relres[r] = sqrt(t0) / sqrt(st.bnorm2[r]);
+  }
+}
+
+__global__ void any_active_kernel(PcgState st) {
+  int a = 0;
+  for (int r = 0; r < st.k; ++r) a |= st.active[r];
+  *st.any_active = a;
+}
+
+// p = beta p + z (p = z on the first iteration), only for active right-hand sides.
+__global__ void pupdate_kernel(int64_t nk, PcgState st, int first, double *p, const double *z) {
+  if (!*st.any_active) return;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nk) return;
+  int r = (int)(i % st.k);
+  if (!st.active[r]) return;
+  if (first) p[i] = z[i];
+  else p[i] = st.beta[r] * p[i] + 1.0 * z[i];
+}
+
+__global__ void init_kernel(int64_t nk, const double *b, double *x, double *r) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nk) return;
+  x[i] = 0.0;
+  r[i] = b[i];
+}
+
+}  // namespace
+
+// ---- plan construction -----------------------------------------------------------
+
+static void build_dir(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, int64_t n,
+                      const std::vector<TreeNode> &nodes, bool upper, DirPlan &D, int64_t &dag,
+                      cudaStream_t s) {
+  // node order: forward = deepest first, backward = root first
+  int maxdepth = 1;
+  for (auto &nd : nodes) maxdepth = std::max(maxdepth, nd.depth);
+  std::vector<int> order;
+  D.stage_ptr.assign(1, 0);
+  D.stage_maxrows.clear();
+  for (int st = 0; st < maxdepth; ++st) {
+    int depth = upper ? st + 1 : maxdepth - st;
+    int64_t mr = 0;
+    for (size_t k = 0; k < nodes.size(); ++k)
+      if (nodes[k].depth == depth) {
+        order.push_back((int)k);
+        mr = std::max(mr, std::min(nodes[k].end, n) - nodes[k].begin);
+      }
+    D.stage_ptr.push_back((int)order.size());
+    D.stage_maxrows.push_back((int)mr);
+  }
+  const int nn = (int)order.size();
+  std::vector<int64_t> nb(nn), ne(nn);
+  for (int k = 0; k < nn; ++k) {
+    nb[k] = nodes[order[k]].begin;
+    ne[k] = std::min(nodes[order[k]].end, n);
+    if (ne[k] < nb[k]) ne[k] = nb[k];
+  }
+  std::vector<int32_t> split(n), level(n, 0), rows(n);
+  std::vector<int64_t> nlev(nn, 0);
+  // split and levels per node (independent across nodes)
+  parallel_for(nn, [&](int64_t k0, int64_t k1) {
+    for (int64_t k = k0; k < k1; ++k) {
+      int64_t b = nb[k], e = ne[k];
+      int64_t ml = -1;
+      if (!upper) {
+        for (int64_t i = b; i < e; ++i) {
+          int64_t q = rp[i], q1 = rp[i + 1] - 1;
+          while (q < q1 && ci[q] < b) ++q;
+          split[i] = (int32_t)(q - rp[i]);
+          int lv = 0;
+          for (; q < q1; ++q) lv = std::max(lv, level[ci[q]] + 1);
+          level[i] = lv;
+          ml = std::max<int64_t>(ml, lv);
+        }
+      } else {
+        for (int64_t i = e - 1; i >= b; --i) {
+          int64_t q = rp[i] + 1, q1 = rp[i + 1];
+          int lv = 0;
+          for (; q < q1 && ci[q] < e; ++q) lv = std::max(lv, level[ci[q]] + 1);
+          split[i] = (int32_t)(q - rp[i]);
+          level[i] = lv;
+          ml = std::max<int64_t>(ml, lv);
+        }
+      }
+      nlev[k] = ml + 1;
+    }
+  }, 1);
+  std::vector<int64_t> lvl_off(nn + 1, 0);
+  for (int k = 0; k < nn; ++k) lvl_off[k + 1] = lvl_off[k] + nlev[k];
+  std::vector<int64_t> level_ptr(lvl_off[nn] + 1, 0);
+  // counting sort of each node's rows by level (rows of a node are contiguous)
+  parallel_for(nn, [&](int64_t k0, int64_t k1) {
+    for (int64_t k = k0; k < k1; ++k) {
+      int64_t b = nb[k], e = ne[k], L = nlev[k];
+      std::vector<int64_t> cnt(L + 1, 0);
+      for (int64_t i = b; i < e; ++i) cnt[level[i] + 1]++;
+      for (int64_t l = 0; l < L; ++l) cnt[l + 1] += cnt[l];
+      for (int64_t l = 0; l < L; ++l) level_ptr[lvl_off[k] + l] = b + cnt[l];
+      std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+      for (int64_t i = b; i < e; ++i) rows[b + pos[level[i]]++] = (int32_t)i;
+    }
+  }, 1);
+  // the level_ptr entry after a node's last level is the next node's first
+  // (or n); fill the closing entries per node
+  {
+    std::vector<int64_t> lp(lvl_off[nn] + nn + 1);
+    // re-pack with explicit end markers: node k levels at [lvl_off[k]+k, ...]
+    std::vector<int64_t> off2(nn + 1, 0);
+    for (int k = 0; k < nn; ++k) off2[k + 1] = off2[k] + nlev[k] + 1;
+    for (int k = 0; k < nn; ++k) {
+      for (int64_t l = 0; l < nlev[k]; ++l) lp[off2[k] + l] = level_ptr[lvl_off[k] + l];
+      lp[off2[k] + nlev[k]] = ne[k];
+    }
+    // lvl_off now indexes level starts; node k has levels [off2[k], off2[k+1]-1)
+    std::vector<int64_t> lo(nn + 1);
+    for (int k = 0; k <= nn; ++k) lo[k] = off2[k];
+    level_ptr.swap(lp);
+    lvl_off.swap(lo);
+  }
+  int64_t crit = 0;
+  for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
+    int64_t m = 0;
+    for (int k = D.stage_ptr[st]; k < D.stage_ptr[st + 1]; ++k) m = std::max(m, nlev[k]);
+    crit += m;
+  }
+  D.crit_levels = crit;
+  // DAG depth of the whole solve (for reporting)
+  {
+    std::vector<int32_t> lv(n, 0);
+    int32_t mx = 0;
+    if (!upper) {
+      for (int64_t i = 0; i < n; ++i) {
+        int32_t l = 0;
+        for (int64_t q = rp[i]; q < rp[i + 1] - 1; ++q) l = std::max(l, lv[ci[q]] + 1);
+        lv[i] = l;
+        mx = std::max(mx, l);
+      }
+    } else {
+      for (int64_t i = n - 1; i >= 0; --i) {
+        int32_t l = 0;
+        for (int64_t q = rp[i] + 1; q < rp[i + 1]; ++q) l = std::max(l, lv[ci[q]] + 1);
+        lv[i] = l;
+        mx = std::max(mx, l);
+      }
+    }
+    dag = (int64_t)mx + 1;
+  }
+  D.nb.upload(nb.data(), nn, s);
+  D.ne.upload(ne.data(), nn, s);
+  // lvl_off for the kernel: node k has levels [lvl_off[k], lvl_off[k+1]-1)
+  // (the last entry of each node's range is its end marker)
+  std::vector<int64_t> lo_kernel(nn + 1);
+  for (int k = 0; k <= nn; ++k) lo_kernel[k] = lvl_off[k];
+  D.lvl_off.upload(lo_kernel.data(), nn + 1, s);
+  D.level_ptr.upload(level_ptr.data(), level_ptr.size(), s);
+  D.rows.upload(rows.data(), n, s);
+  D.split.upload(split.data(), n, s);
+  RCHOL_CUDA(cudaStreamSynchronize(s));
+}
+
+namespace {
+
+__global__ void transpose_count_kernel(int64_t nnz, const int32_t *uci, unsigned long long *cnt) {
+  int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q < nnz) atomicAdd(&cnt[uci[q]], 1ull);
+}
+
+__global__ void transpose_scatter_kernel(int64_t n, const int64_t *urp, const int32_t *uci,
+                                         const double *uv, const int64_t *lrp,
+                                         unsigned long long *cur, int32_t *tci, double *tv) {
+  int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  for (int64_t q = urp[row] + lane; q < urp[row + 1]; q += 32) {
+    int32_t j = uci[q];
+    unsigned long long slot = atomicAdd(&cur[j], 1ull);
+    tci[lrp[j] + slot] = (int32_t)row;
+    tv[lrp[j] + slot] = uv[q];
+  }
+}
+
+// Sort each row of L by column (rank sort; columns within a row are unique).
+__global__ void row_sort_kernel(int64_t n, const int64_t *lrp, const int32_t *tci, const double *tv,
+                                int32_t *lci, double *lv) {
+  int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  int64_t b = lrp[row], e = lrp[row + 1];
+  for (int64_t q = b + lane; q < e; q += 32) {
+    int32_t c = tci[q];
+    int64_t rank = 0;
+    for (int64_t f = b; f < e; ++f) rank += (tci[f] < c);
+    lci[b + rank] = c;
+    lv[b + rank] = tv[q];
+  }
+}
+
+__global__ void diag_inverse_kernel(int64_t n, const int64_t *urp, const double *uv, double *dinv,
+                                    float *dinv32, const float *uv32) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dinv[i] = 1.0 / uv[urp[i]];
+  if (dinv32) dinv32[i] = 1.0f / uv32[urp[i]];
+}
+
+__global__ void to_f32_kernel(int64_t n, const double *a, float *b) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+__global__ void i64_from_ull_kernel(int64_t n, const unsigned long long *a, int64_t *b) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (int64_t)a[i];
+}
+
+}  // namespace
+
+void finish_factor(rchol_factor_s &F, cudaStream_t s) {
+  const int64_t n = F.n, nnz = F.nnz;
+  // L = transpose(U)
+  DevBuf<unsigned long long> cnt(n);
+  RCHOL_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), s));
+  transpose_count_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, F.uci.p, cnt.p);
+  F.lrp.alloc(n + 1);
+  i64_from_ull_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, cnt.p, F.lrp.p);
+  RCHOL_CUDA(cudaGetLastError());
+  exclusive_scan_i64(F.lrp.p, n, s);
+  RCHOL_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), s));
+  {
+    DevBuf<int32_t> tci(nnz);
+    DevBuf<double> tv(nnz);
+    transpose_scatter_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(
+        n, F.urp.p, F.uci.p, F.uv.p, F.lrp.p, cnt.p, tci.p, tv.p);
+    F.lci.alloc(nnz);
+    F.lv.alloc(nnz);
+    row_sort_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(n, F.lrp.p, tci.p, tv.p, F.lci.p,
+                                                                      F.lv.p);
+    RCHOL_CUDA(cudaGetLastError());
+    RCHOL_CUDA(cudaStreamSynchronize(s));
+  }
+  if (F.precision == RCHOL_PREC_FP32) {
+    F.uv32.alloc(nnz);
+    F.lv32.alloc(nnz);
+    to_f32_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, F.uv.p, F.uv32.p);
+    to_f32_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, F.lv.p, F.lv32.p);
+    RCHOL_CUDA(cudaGetLastError());
+  }
+  build_plan(F, s);
+}
+
+void build_plan(rchol_factor_s &F, cudaStream_t s) {
+  const int64_t n = F.n, nnz = F.nnz;
+  auto P = new SolvePlan();
+  try {
+    std::vector<int64_t> rp(n + 1);
+    std::vector<int32_t> ci(nnz);
+    F.lrp.download(rp.data(), n + 1, s);
+    F.lci.download(ci.data(), nnz, s);
+    RCHOL_CUDA(cudaStreamSynchronize(s));
+    build_dir(rp, ci, n, F.nodes, false, P->fwd, P->dag_fwd, s);
+    F.urp.download(rp.data(), n + 1, s);
+    F.uci.download(ci.data(), nnz, s);
+    RCHOL_CUDA(cudaStreamSynchronize(s));
+    build_dir(rp, ci, n, F.nodes, true, P->bwd, P->dag_bwd, s);
+    P->dinv.alloc(n);
+    if (F.precision == RCHOL_PREC_FP32) P->dinv32.alloc(n);
+    diag_inverse_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+        n, F.urp.p, F.uv.p, P->dinv.p, P->dinv32.p, F.uv32.p);
+    RCHOL_CUDA(cudaGetLastError());
+    RCHOL_CUDA(cudaStreamSynchronize(s));
+  } catch (...) {
+    delete P;
+    throw;
+  }
+  destroy_plan(F.plan);
+  F.plan = P;
+}
+
+static void ensure_scratch(SolvePlan &P, bool fp32, int64_t count) {
+  if (fp32) {
+    if (P.scratch32.n < (size_t)count) P.scratch32.alloc(count);
+    if (P.ytmp32.n < (size_t)count) P.ytmp32.alloc(count);
+  } else {
+    if (P.scratch.n < (size_t)count) P.scratch.alloc(count);
+    if (P.ytmp.n < (size_t)count) P.ytmp.alloc(count);
+  }
+}
+
+void trsv(const rchol_factor_s &F, bool upper, const double *in, double *out, int k, cudaStream_t s) {
+  SolvePlan &P = *F.plan;
+  bool fp32 = F.precision == RCHOL_PREC_FP32;
+  ensure_scratch(P, fp32, F.n * k);
+  if (fp32) run_trsv<float, double, double>(F, P, upper, in, out, k, s);
+  else run_trsv<double, double, double>(F, P, upper, in, out, k, s);
+}
+
+void precond(const rchol_factor_s &F, const double *r, double *z, int k, cudaStream_t s) {
+  SolvePlan &P = *F.plan;
+  bool fp32 = F.precision == RCHOL_PREC_FP32;
+  ensure_scratch(P, fp32, F.n * k);
+  if (fp32) {
+    run_trsv<float, double, float>(F, P, false, r, P.ytmp32.p, k, s);
+    run_trsv<float, float, double>(F, P, true, P.ytmp32.p, z, k, s);
+  } else {
+    run_trsv<double, double, double>(F, P, false, r, P.ytmp.p, k, s);
+    run_trsv<double, double, double>(F, P, true, P.ytmp.p, z, k, s);
+  }
+}
+
+void spmv_public(const rchol_matrix_s &A, const double *x, double *y, int k, cudaStream_t s) {
+  spmv(A, x, y, k, s);
+}
+
+int64_t plan_levels(const rchol_factor_s &F, bool upper) {
+  return upper ? F.plan->dag_bwd : F.plan->dag_fwd;
+}
+
+// PCG for k right-hand sides (device pointers), c++/util/pcg.cpp:57-127.
+void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x,
+                int k, double tol, int maxit, double *relres, int *itr, cudaStream_t s) {
+  const int64_t n = A.n, nk = n * k;
+  DevBuf<double> r(nk), z(nk), p(nk), q(nk);
+  DevBuf<double> sc(8 * (size_t)k + 2 * (size_t)RED_BLOCKS * k + k);
+  DevBuf<int> ic(2 * (size_t)k + 1);
+  RCHOL_CUDA(cudaMemsetAsync(sc.p, 0, sc.bytes(), s));
+  RCHOL_CUDA(cudaMemsetAsync(ic.p, 0, ic.bytes(), s));
+  PcgState st;
+  st.bnorm2 = sc.p;
+  st.rnorm2 = sc.p + k;
+  st.rz = sc.p + 2 * k;
+  st.rz_prev = sc.p + 3 * k;
+  st.pr = sc.p + 4 * k;
+  st.pq = sc.p + 5 * k;
+  st.alpha = sc.p + 6 * k;
+  st.beta = sc.p + 7 * k;
+  st.partial = sc.p + 8 * k;
+  double *d_relres = sc.p + 8 * k + 2 * (size_t)RED_BLOCKS * k;
+  st.active = ic.p;
+  st.iters = ic.p + k;
+  st.any_active = ic.p + 2 * k;
+  st.k = k;
+  st.tol = tol;
+  st.maxit = maxit;
+  const unsigned eb = (unsigned)((nk + 255) / 256);
+  init_kernel<<<eb, 256, 0, s>>>(nk, b, x, r.p);
+  // ||b||^2 through the residual reduction (b - 0), which runs before any
+  // right-hand side is marked active
+  RCHOL_CUDA(cudaMemsetAsync(q.p, 0, q.bytes(), s));
+  reduce_kernel<RED_RESID><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, b, q.p, nullptr, nullptr, nullptr);
+  finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_INIT, 0, nullptr);
+  RCHOL_CUDA(cudaGetLastError());
+  int h_any = 1;
+  for (int it = 0; it < maxit; ++it) {
+    const int first = it == 0;
+    precond(F, r.p, z.p, k, s);
+    reduce_kernel<RED_DOT><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, r.p, z.p, nullptr, nullptr, nullptr);
+    finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_BETA, first, nullptr);
+    pupdate_kernel<<<eb, 256, 0, s>>>(nk, st, first, p.p, z.p);
+    spmv(A, p.p, q.p, k, s);
+    reduce_kernel<RED_DOT2><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, p.p, q.p, nullptr, nullptr, r.p);
+    finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_ALPHA, first, nullptr);
+    reduce_kernel<RED_UPDATE><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, p.p, q.p, x, r.p, nullptr);
+    finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_CONV, first, nullptr);
+    any_active_kernel<<<1, 1, 0, s>>>(st);
+    RCHOL_CUDA(cudaGetLastError());
+    if ((it & 3) == 3 || it + 1 == maxit) {
+      RCHOL_CUDA(cudaMemcpyAsync(&h_any, st.any_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+      RCHOL_CUDA(cudaStreamSynchronize(s));
+      if (!h_any) break;
+    }
+  }
+  // relres = ||A x - b|| / ||b||
+  spmv(A, x, q.p, k, s);
+  reduce_kernel<RED_RESID><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, q.p, b, nullptr, nullptr, nullptr);
+  finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_RESID, 0, d_relres);
+  RCHOL_CUDA(cudaGetLastError());
+  RCHOL_CUDA(cudaMemcpyAsync(relres, d_relres, k * sizeof(double), cudaMemcpyDeviceToHost, s));
+  RCHOL_CUDA(cudaMemcpyAsync(itr, st.iters, k * sizeof(int), cudaMemcpyDeviceToHost, s));
+  RCHOL_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace rchol
