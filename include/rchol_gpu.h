@@ -65,6 +65,13 @@ int64_t rchol_gpu_tree_num_parts(rchol_tree_t tree); /* length of part */
 int rchol_gpu_tree_get(rchol_tree_t tree, int64_t *perm, int64_t *part);
 void rchol_gpu_tree_destroy(rchol_tree_t tree);
 
+/* B = A(perm, perm) with sorted rows, on the host (c++/util/util.cpp:16-49,
+ * used by c++/ex_laplace_parallel.cpp:38).  B has A's nnz; the out arrays
+ * must hold n+1, nnz and nnz entries. */
+int rchol_gpu_reorder(int64_t n, const int64_t *row_ptr, const int64_t *col_idx,
+                      const double *val, const int64_t *perm, int64_t *out_row_ptr,
+                      int64_t *out_col_idx, double *out_val);
+
 /* ---- matrices --------------------------------------------------------------
  * Upload an SDDM matrix.  With a tree, the matrix is stored permuted, A(p,p)
  * (c++/util/util.cpp:16-49), which is the system pcg() solves in the

@@ -35,10 +35,16 @@ SparseCSR remove_diagonal(const SparseCSR &A, std::vector<size_t> &rowPtr,
 
 namespace {
 
+// Discards everything.  It keeps no put area, so the reference's worker
+// threads can write to it concurrently (a stringbuf would race).
+struct NullBuf : std::streambuf {
+  int overflow(int c) override { return c == EOF ? 0 : c; }
+};
+
 struct Quiet {
-  std::ostringstream sink;
+  NullBuf sink;
   std::streambuf *old;
-  Quiet() : old(std::cout.rdbuf(sink.rdbuf())) {}
+  Quiet() : old(std::cout.rdbuf(&sink)) {}
   ~Quiet() { std::cout.rdbuf(old); }
 };
 

@@ -33,6 +33,7 @@ SIGNATURES = [
     ("rchol_gpu_tree_num_parts", _i64, [_vp]),
     ("rchol_gpu_tree_get", C.c_int, [_vp, _i64p, _i64p]),
     ("rchol_gpu_tree_destroy", None, [_vp]),
+    ("rchol_gpu_reorder", C.c_int, [_i64, _i64p, _i64p, _dp, _i64p, _i64p, _i64p, _dp]),
     ("rchol_gpu_matrix_create", C.c_int, [_i64, _i64p, _i64p, _dp, _vp, C.POINTER(_vp)]),
     ("rchol_gpu_matrix_size", _i64, [_vp]),
     ("rchol_gpu_matrix_nnz", _i64, [_vp]),
@@ -151,6 +152,15 @@ class Tree(Handle):
         part = np.zeros(np_, np.int64)
         check(lib().rchol_gpu_tree_get(self.ptr, p64(perm), p64(part)))
         return perm, part
+
+
+def reorder(rowptr, colidx, val, perm):
+    """B = A(perm, perm) on the host through the C ABI (c++/util/util.cpp:16-49)."""
+    rp, ci, v, p = i64(rowptr), i64(colidx), f64(val), i64(perm)
+    n, nnz = len(rp) - 1, int(rp[-1])
+    orp, oci, ov = np.zeros(n + 1, np.int64), np.zeros(nnz, np.int64), np.zeros(nnz)
+    check(lib().rchol_gpu_reorder(n, p64(rp), p64(ci), pd(v), p64(p), p64(orp), p64(oci), pd(ov)))
+    return orp, oci, ov
 
 
 class Matrix(Handle):

@@ -85,6 +85,24 @@ int rchol_gpu_tree_get(rchol_tree_t t, int64_t *perm, int64_t *part) {
 
 void rchol_gpu_tree_destroy(rchol_tree_t t) { delete t; }
 
+int rchol_gpu_reorder(int64_t n, const int64_t *row_ptr, const int64_t *col_idx, const double *val,
+                      const int64_t *perm, int64_t *out_row_ptr, int64_t *out_col_idx,
+                      double *out_val) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(val && perm && out_row_ptr && out_col_idx && out_val, "null argument");
+  validate_csr(n, row_ptr, col_idx);
+  std::vector<char> seen(n, 0);
+  for (int64_t i = 0; i < n; ++i) {
+    RCHOL_CHECK_ARG(perm[i] >= 0 && perm[i] < n && !seen[perm[i]], "perm is not a permutation");
+    seen[perm[i]] = 1;
+  }
+  HostCsr B = reorder(n, row_ptr, col_idx, val, std::vector<int64_t>(perm, perm + n));
+  std::memcpy(out_row_ptr, B.rp.data(), (n + 1) * sizeof(int64_t));
+  std::memcpy(out_col_idx, B.ci.data(), B.ci.size() * sizeof(int64_t));
+  std::memcpy(out_val, B.v.data(), B.v.size() * sizeof(double));
+  API_END
+}
+
 // ---- matrices ---------------------------------------------------------------
 
 int rchol_gpu_matrix_create(int64_t n, const int64_t *row_ptr, const int64_t *col_idx,

@@ -212,12 +212,12 @@ __global__ void spmv1_kernel(int64_t n, const int64_t *__restrict__ rp, const in
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int64_t row = t / LPR;
   int sub = (int)(t % LPR);
-  if (row >= n) return;
   double s = 0.0;
-  for (int64_t q = rp[row] + sub; q < rp[row + 1]; q += LPR) s += v[q] * x[ci[q]];
+  if (row < n)  // no early return: every lane takes part in the shuffles
+    for (int64_t q = rp[row] + sub; q < rp[row + 1]; q += LPR) s += v[q] * x[ci[q]];
 #pragma unroll
   for (int o = LPR / 2; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
-  if (sub == 0) y[row] = s;
+  if (sub == 0 && row < n) y[row] = s;
 }
 
 // y = A x for k right-hand sides stored row-major; one warp per row, lanes over k.

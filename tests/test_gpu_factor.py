@@ -1,0 +1,139 @@
+"""GPU factorization (through the C ABI) against the oracle.
+
+* Bit-exact: the GPU factor equals the oracle's device contract (same Philox
+  stream, same merge/sort/scan order) for every case.
+* Integer work: ordering and nonzero pattern are exact; the nonzero count of
+  G matches the reference factor within 5% (different random stream).
+* Method guarantees: E[G G^T] -> A (unbiasedness, 256 seeds on a small grid)
+  at the reference's own rate, and PCG iteration counts within 10% of the
+  reference's, every final residual recomputed on the host in FP64.
+"""
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+from rchol_gb300 import generators
+from conftest import csr_u64
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_factor(R, A, threads, seed, precision=0):
+    tree = R.Tree.build(A.indptr, A.indices, threads)
+    Ad = R.Matrix.create(A.indptr, A.indices, A.data, tree)
+    F = R.Factor.compute(Ad, tree, seed=seed, precision=precision)
+    return tree, Ad, F
+
+
+CASES = [
+    ("lap8_t1", lambda: generators.laplace_3d(8), 1),
+    ("lap10_t8", lambda: generators.laplace_3d(10), 8),
+    ("lap16_t32", lambda: generators.laplace_3d(16), 32),
+    ("weighted12_t16", lambda: generators.laplace_3d_weighted(12, sigma=1.0, seed=3), 16),
+    ("grid2d_t8", lambda: generators.grid_2d_weighted(40, 33, "loguniform", shift=1e-4, dirichlet=False, seed=1), 8),
+    ("checker16_t8", lambda: generators.checkerboard_3d(16, block=4), 8),
+]
+
+
+@pytest.mark.parametrize("name,make,threads", CASES, ids=[c[0] for c in CASES])
+def test_factor_bit_exact_vs_device_contract(cuda, O, R, name, make, threads):
+    A = make()
+    tree, Ad, F = gpu_factor(R, A, threads, seed=12345)
+    perm, part = tree.arrays()
+    Au = csr_u64(A)
+    Ap = O.reorder(Au, perm.astype(np.uint64))
+    Go, d, singular = O.factor(O.extend(Ap), part.astype(np.uint64), oracle.MODE_DEVICE, 12345)
+    assert not singular
+    grp, gci, gv = F.export()
+    assert np.array_equal(grp, Go[0].astype(np.int64))
+    assert np.array_equal(gci, Go[1].astype(np.int64))
+    assert np.array_equal(gv, Go[2])
+    assert np.array_equal(F.pivots(), d[:-1])
+
+
+def test_factor_structure(cuda, R):
+    A = generators.laplace_3d(12)
+    tree, Ad, F = gpu_factor(R, A, 8, seed=1)
+    rp, ci, v = F.export()
+    n = A.shape[0]
+    for i in range(0, n, 37):
+        row = ci[rp[i]:rp[i + 1]]
+        assert row[0] == i and v[rp[i]] > 0  # diagonal first, positive
+        assert np.all(np.diff(row) > 0)       # strictly increasing (upper triangular)
+    assert ci.max() < n
+
+
+def test_nnz_within_5pct_of_reference(cuda, O, R):
+    A = generators.laplace_3d(20)
+    Au = csr_u64(A)
+    for threads in (4, 16):
+        tree, Ad, F = gpu_factor(R, A, threads, seed=5)
+        Gref, _, _, _ = O.rchol(Au, threads, seed=5, mode=oracle.MODE_REF)  # == reference (pinned)
+        assert abs(F.nnz - len(Gref[1])) / len(Gref[1]) < 0.05
+
+
+def test_unbiased_256_seeds(cuda, R):
+    """||mean_k G_k G_k^T - A|| / ||A|| decays like 1/sqrt(K); the reference
+    gives 0.0092 at K=256 on the 6^3 grid."""
+    A = generators.laplace_3d(6)
+    tree = R.Tree.build(A.indptr, A.indices, 2)
+    perm, part = tree.arrays()
+    Ap = A[perm][:, perm].toarray()
+    Ad = R.Matrix.create(A.indptr, A.indices, A.data, tree)
+    acc = np.zeros_like(Ap)
+    errs = {}
+    for k in range(256):
+        F = R.Factor.compute(Ad, tree, seed=1000 + k)
+        rp, ci, v = F.export()
+        Gt = sp.csr_matrix((v, ci, rp), shape=Ap.shape).toarray()
+        acc += Gt.T @ Gt
+        if k + 1 in (16, 256):
+            errs[k + 1] = np.linalg.norm(acc / (k + 1) - Ap) / np.linalg.norm(Ap)
+    assert errs[256] < 0.02
+    assert errs[256] < errs[16] / 2.5
+
+
+@pytest.mark.parametrize("n,threads", [(16, 8), (24, 32)])
+def test_pcg_iterations_within_10pct(cuda, O, R, n, threads):
+    A = generators.laplace_3d(n)
+    Au = csr_u64(A)
+    b = np.random.default_rng(7).uniform(-1, 1, A.shape[0])
+    its_gpu, its_ref = [], []
+    for seed in range(4):
+        tree, Ad, F = gpu_factor(R, A, threads, seed=seed)
+        perm, part = tree.arrays()
+        bp = b[perm]
+        x, relres, itr = R._pcg_host(Ad, F, bp.reshape(-1, 1), 1e-10, 200)
+        Ap = A[perm][:, perm]
+        true_rel = np.linalg.norm(Ap @ x[:, 0] - bp) / np.linalg.norm(bp)  # FP64 host check
+        assert true_rel < 1e-9 and abs(true_rel - relres[0]) < 1e-12
+        its_gpu.append(int(itr[0]))
+        Gr, pr, _, _ = O.rchol(Au, threads, seed=seed, mode=oracle.MODE_REF)
+        _, _, ito = O.pcg(O.reorder(Au, pr), bp, 1e-10, 200, Gr)
+        its_ref.append(ito)
+    assert abs(np.mean(its_gpu) - np.mean(its_ref)) <= 0.1 * np.mean(its_ref) + 1
+
+
+def test_fp32_factor_values(cuda, R):
+    A = generators.laplace_3d(10)
+    _, _, F64 = gpu_factor(R, A, 8, seed=3)
+    _, _, F32 = gpu_factor(R, A, 8, seed=3, precision=1)
+    a, b = F64.export(), F32.export()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+
+
+def test_singular_matrix_reports_error(cuda, R):
+    # pure Laplacian (zero row sums): no ground edge anywhere -> zero pivot
+    n = 30
+    e = np.arange(n - 1)
+    L = sp.coo_matrix((-np.ones(n - 1), (e, e + 1)), shape=(n, n))
+    L = L + L.T
+    L = L - sp.diags(np.asarray(L.sum(axis=1)).ravel())
+    L = sp.csr_matrix(L)
+    L.sort_indices()
+    tree = R.Tree.build(L.indptr, L.indices, 1)
+    Ad = R.Matrix.create(L.indptr, L.indices, L.data, tree)
+    with pytest.raises(R.RcholError, match="zero pivot"):
+        R.Factor.compute(Ad, tree, seed=0)

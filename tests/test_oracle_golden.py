@@ -1,0 +1,74 @@
+"""The oracle restatement reproduces the reference's own outputs (golden
+fixtures generated from the unmodified reference by tests/golden/make_golden.py)
+bit for bit: ordering, permuted matrix, extended Laplacian, factor G for a
+fixed sampler seed, and the PCG solution / residual / iteration count."""
+
+import os
+import platform
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_golden
+
+import oracle
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_oracle_matches_golden(O, path):
+    g = load_golden(path)
+    A = (g["A_rp"], g["A_ci"], g["A_v"])
+    threads = int(g["threads"])
+    if threads:
+        if str(g["arch"]) == platform.machine():
+            perm, ridx = O.order(A, threads)
+            assert np.array_equal(perm, g["perm"])
+            assert np.array_equal(ridx, g["ridx"])
+        Ap = O.reorder(A, g["perm"])
+        for got, want in zip(Ap, (g["Ap_rp"], g["Ap_ci"], g["Ap_v"])):
+            assert np.array_equal(got, want)
+    else:
+        Ap = A
+    L = O.extend(Ap)
+    for got, want in zip(L, (g["L_rp"], g["L_ci"], g["L_v"])):
+        assert np.array_equal(got, want)
+    G, d, singular = O.factor(L, g["ridx"], oracle.MODE_REF, int(g["seed"]))
+    assert not singular
+    for got, want in zip(G, (g["G_rp"], g["G_ci"], g["G_v"])):
+        assert np.array_equal(got, want)
+    x, relres, itr = O.pcg(Ap, g["b"], float(g["tol"]), 200, G)
+    assert itr == int(g["itr"])
+    assert relres == float(g["relres"])
+    assert np.array_equal(x, g["x"])
+
+
+def test_philox_known_answers(O):
+    # Random123 known-answer vectors for philox4x32-10
+    assert [hex(v) for v in O.philox([0, 0, 0, 0], [0, 0])] == ["0x6627e8d5", "0xe169c58d", "0xbc57ac4c", "0x9b00dbd8"]
+    assert [hex(v) for v in O.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2)] == [
+        "0x408f276d", "0x41c83b0e", "0xa20bc7c6", "0x6d5451fd"]
+    assert [hex(v) for v in O.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344],
+                                     [0xA4093822, 0x299F31D0])] == [
+        "0xd16cfe09", "0x94fdcceb", "0x5001e420", "0x24126ea1"]
+
+
+def test_uniform_range(O):
+    u = np.array([O.uniform(5, v, i) for v in range(50) for i in range(40)])
+    assert u.min() >= 0.0 and u.max() < 1.0
+    assert abs(u.mean() - 0.5) < 0.03
+
+
+def test_device_mode_is_schedule_free(O):
+    """The device contract does not depend on the tree partition: the same
+    permutation factored with different result_idx gives the same G."""
+    from rchol_gb300 import generators
+
+    A = generators.laplace_3d(8)
+    Au = (A.indptr.astype(np.uint64), A.indices.astype(np.uint64), A.data)
+    perm, ridx = O.order(Au, 4)
+    L = O.extend(O.reorder(Au, perm))
+    n = len(perm)
+    G1, _, _ = O.factor(L, ridx, oracle.MODE_DEVICE, 3)
+    G2, _, _ = O.factor(L, np.array([0, n + 1], dtype=np.uint64), oracle.MODE_DEVICE, 3)
+    for a, b in zip(G1, G2):
+        assert np.array_equal(a, b)
