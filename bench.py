@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""PCG time to a 1e-8 relative residual on one GB300: FP32-G vs FP64 vs CPU.
+
+Workload: 3D 7-point graph Laplacian on a 256^3 grid (16.8M unknowns) with
+edge weights exp(N(0,1)) and diagonal = sum of incident weights + 1e-3
+(SDDM), b ~ N(0,1); nested-dissection ordering (METIS, host), randomized
+Cholesky factor on the GPU (FP64 accumulation), PCG to 1e-8 verified in FP64.
+A "step" is one complete PCG solve.  ``value`` is the FP32-G solve time with
+A, G and b resident in HBM; ``e2e`` is the same solve through the C ABI with
+host buffers (b copied in, x copied out inside the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: the path does not shard (one GPU, no sharding), so N ranks run N
+independent replicas; ``value`` is then the time of the slowest replica and
+the line reports the aggregate throughput in ``solves_per_s``.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PCG time to 1e-8 residual: FP32-G vs FP64 GPU vs CPU; SpMV/SpTRSV HBM GB/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=256, help="grid side")
+    p.add_argument("--leaves", type=int, default=2048, help="nested-dissection subdomains")
+    p.add_argument("--tol", type=float, default=1e-8)
+    p.add_argument("--maxit", type=int, default=200)
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--cpu-sample-iters", type=int, default=2)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1 and args.impl == "gb300":
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend)
+        pg = dist
+    return rank, local, world, pg
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per triangular solve from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "trsv_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def build_problem(args):
+    from rchol_gb300 import generators
+
+    t0 = time.time()
+    A = generators.laplace_3d_weighted(args.n, sigma=1.0, shift=1e-3, seed=args.seed)
+    b = np.random.default_rng(args.seed + 1).standard_normal(A.shape[0])
+    return A, b, time.time() - t0
+
+
+# --------------------------------------------------------------------------------------
+# GB300 arm
+# --------------------------------------------------------------------------------------
+
+def run_gb300(args, rank, local, world, pg):
+    import torch
+
+    import rchol_gb300 as R
+    from rchol_gb300 import _lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = _lib.lib()
+    A, b, t_gen = build_problem(args)
+    n = A.shape[0]
+    t0 = time.time()
+    tree = R.Tree.build(A.indptr, A.indices, args.leaves)
+    perm, part = tree.arrays()
+    t_order = time.time() - t0
+    t0 = time.time()
+    Ad = R.Matrix.create(A.indptr, A.indices, A.data, tree)
+    torch.cuda.synchronize()
+    t_upload = time.time() - t0
+    t0 = time.time()
+    F64 = R.Factor.compute(Ad, tree, seed=args.seed, precision=R.PREC_FP64)
+    torch.cuda.synchronize()
+    t_factor = time.time() - t0
+    F32 = R.Factor.compute(Ad, tree, seed=args.seed, precision=R.PREC_FP32)
+    nnzG = F64.nnz
+    nnzA = A.nnz
+    bp = np.ascontiguousarray(b[perm])
+    d_b = torch.tensor(bp, dtype=torch.float64, device=dev)
+    d_x = torch.zeros_like(d_b)
+    stream = torch.cuda.current_stream(dev)
+    relres = np.zeros(1)
+    itr = np.zeros(1, dtype=np.int32)
+
+    def solve(F):
+        _lib.check(L.rchol_gpu_pcg_d(Ad.ptr, F.ptr, d_b.data_ptr(), d_x.data_ptr(), 1, args.tol, args.maxit,
+                                     _lib.pd(relres), itr.ctypes.data_as(_lib._ip), stream.cuda_stream))
+        return float(relres[0]), int(itr[0])
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize(dev)
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = None
+        for _ in range(steps):
+            out = fn()
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        if pg is not None:
+            t = torch.tensor([ms], device=dev)
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, out
+
+    launches0 = L.rchol_gpu_launch_count()
+    with ClockSampler(local) as clk:
+        ms32, (rr32, it32) = timed(lambda: solve(F32), args.steps)
+    launches = (L.rchol_gpu_launch_count() - launches0) // (args.steps + args.warmup)
+    x32 = d_x.cpu().numpy()
+    ms64, (rr64, it64) = timed(lambda: solve(F64), args.steps)
+    x64 = d_x.cpu().numpy()
+    # FP64 host verification of both solutions: ||A(p,p) x - b(p)|| / ||b||
+    Ap = A[perm][:, perm].tocsr()
+    ver32 = float(np.linalg.norm(Ap @ x32 - bp) / np.linalg.norm(bp))
+    ver64 = float(np.linalg.norm(Ap @ x64 - bp) / np.linalg.norm(bp))
+
+    # kernel-level rates: one forward triangular solve and one SpMV
+    d_y32 = torch.empty_like(d_b)
+
+    def trsv(F):
+        _lib.check(L.rchol_gpu_trsv_d(F.ptr, 0, d_b.data_ptr(), d_y32.data_ptr(), 1, stream.cuda_stream))
+
+    def spmv():
+        _lib.check(L.rchol_gpu_spmv_d(Ad.ptr, d_b.data_ptr(), d_y32.data_ptr(), 1, stream.cuda_stream))
+
+    trsv32_ms, _ = timed(lambda: trsv(F32), max(3, args.steps))
+    trsv64_ms, _ = timed(lambda: trsv(F64), max(3, args.steps))
+    spmv_ms, _ = timed(spmv, 20)
+    rows = (n + 1) * 8 + 2 * 8 * n  # row pointers + read rhs + write solution
+    bytes_trsv32 = nnzG * (4 + 4) + rows
+    bytes_trsv64 = nnzG * (8 + 4) + rows
+    bytes_spmv = nnzA * (8 + 4) + rows
+    peak, peak_kind = measured_peak_hbm()
+    gbs = lambda by, ms: by / (ms * 1e-3) / 1e9
+
+    # end to end through the C ABI with host buffers
+    x_host = np.zeros(n)
+    rr_h = np.zeros(1)
+    it_h = np.zeros(1, dtype=np.int32)
+
+    def solve_host():
+        _lib.check(L.rchol_gpu_pcg(Ad.ptr, F32.ptr, _lib.pd(bp), _lib.pd(x_host), 1, args.tol, args.maxit,
+                                   _lib.pd(rr_h), it_h.ctypes.data_as(_lib._ip)))
+
+    for _ in range(args.warmup):
+        solve_host()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        solve_host()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if pg is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, Ap, bp, F64, it64)
+    if rank != 0:
+        return None
+    traffic = profile_traffic()
+    line = {
+        "metric": METRIC,
+        "value": round(ms32, 3),
+        "unit": "ms",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms32, 3),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32-G / fp64-PCG",
+        "data": "synthetic (seeded log-normal coefficients, b ~ N(0,1))",
+        "config": {
+            "workload": f"PCG to {args.tol:g}, 7-point log-normal Laplacian {args.n}^3 (n={n}, nnz(A)={nnzA}), "
+                        f"rchol G (nnz={nnzG}) stored and applied in FP32",
+            "grid": args.n, "leaves": args.leaves, "tol": args.tol,
+            "l2": "inputs larger than L2 (A %.2f GB, G %.2f GB)" % (nnzA * 12 / 1e9, nnzG * 8 / 1e9),
+            "parallelism": f"replicas x{world}",
+        },
+        "fp32": {"ms": round(ms32, 3), "iters": it32, "relres_gpu": rr32, "relres_host_fp64": ver32},
+        "fp64": {"ms": round(ms64, 3), "iters": it64, "relres_gpu": rr64, "relres_host_fp64": ver64},
+        "fp32_speedup_vs_fp64": round(ms64 / ms32, 3),
+        "solves_per_s": round(world * 1e3 / ms32, 3),
+        "kernels": {
+            "trsv_fp32": {"ms": round(trsv32_ms, 4), "GB/s": round(gbs(bytes_trsv32, trsv32_ms), 1)},
+            "trsv_fp64": {"ms": round(trsv64_ms, 4), "GB/s": round(gbs(bytes_trsv64, trsv64_ms), 1)},
+            "spmv_fp64": {"ms": round(spmv_ms, 4), "GB/s": round(gbs(bytes_spmv, spmv_ms), 1)},
+        },
+        "roofline": {
+            "kernel": "forward triangular solve with G (fp32), all stage launches",
+            "bound": "hbm",
+            "achieved": round(gbs(bytes_trsv32, trsv32_ms), 1),
+            "peak": peak,
+            "peak_kind": peak_kind,
+            "unit": "GB/s",
+            "frac": round(gbs(bytes_trsv32, trsv32_ms) / peak, 4),
+            "traffic": (traffic or {}).get("bytes_per_solve"),
+        },
+        "setup_s": {"generate": round(t_gen, 2), "order": round(t_order, 2), "upload": round(t_upload, 2),
+                    "factor_gpu": round(t_factor, 2)},
+        "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    return line
+
+
+def cpu_baseline(args, Ap, bp, F64, it64):
+    """The oracle restatement of the reference pcg (pinned bit for bit to the
+    reference) on the host cores: a bounded sample of PCG iterations with the
+    GPU's FP64 factor, scaled to the full iteration count."""
+    import oracle
+
+    O = oracle.Oracle()
+    threads = os.cpu_count() or 1
+    rp, ci, v = F64.export()
+    G = (rp.astype(np.uint64), ci.astype(np.uint64), v)
+    A3 = (Ap.indptr.astype(np.uint64), Ap.indices.astype(np.uint64), Ap.data)
+    S = args.cpu_sample_iters
+    t0 = time.perf_counter()
+    O.pcg(A3, bp, 1e-300, S, G, threads=threads)
+    dt = time.perf_counter() - t0
+    per_iter = dt / S
+    return {"value": round(per_iter * it64 * 1e3, 1), "unit": "ms", "cores": threads, "kind": "port",
+            "sample": f"{S} PCG iterations of the full {args.n}^3 system (oracle restatement of "
+                      f"c++/util/pcg.cpp: serial triangular solves, SpMV/dots on {threads} threads), "
+                      f"{per_iter:.2f} s/iteration scaled by the {it64} iterations the FP64 solve needs"}
+
+
+# --------------------------------------------------------------------------------------
+# reference arm: the reference's CPU implementation (oracle port, pinned bit for bit)
+# --------------------------------------------------------------------------------------
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import oracle
+
+    O = oracle.Oracle()
+    threads = os.cpu_count() or 1
+    t_leaves = 1
+    while t_leaves * 2 <= threads:
+        t_leaves *= 2
+    A, b, _ = build_problem(args)
+    A3 = (A.indptr.astype(np.uint64), A.indices.astype(np.uint64), A.data)
+    t0 = time.time()
+    G, perm, ridx, d = O.rchol(A3, t_leaves, seed=args.seed, mode=oracle.MODE_REF)
+    t_factor = time.time() - t0
+    Ap = O.reorder(A3, perm)
+    bp = np.ascontiguousarray(b[perm.astype(np.int64)])
+    # calibration: the reference's own iteration count to 1e-8 with its own G
+    t0 = time.time()
+    _, relres, iters = O.pcg(Ap, bp, args.tol, args.maxit, G, threads=threads)
+    t_full = time.time() - t0
+    S = args.cpu_sample_iters
+    for _ in range(max(0, args.warmup - 1)):
+        O.pcg(Ap, bp, 1e-300, 1, G, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.pcg(Ap, bp, 1e-300, S, G, threads=threads)
+    per_iter = (time.perf_counter() - t0) / (args.steps * S)
+    value = per_iter * iters * 1e3
+    return {
+        "metric": METRIC, "impl": "reference", "value": round(value, 1), "unit": "ms", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(value, 1), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (same seeds as the gb300 arm)",
+        "config": {"workload": f"PCG to {args.tol:g}, 7-point log-normal Laplacian {args.n}^3, reference rchol G "
+                               f"(nnz={len(G[1])}, {t_leaves} subdomains)", "grid": args.n, "tol": args.tol},
+        "iters": int(iters), "relres": relres, "full_solve_s": round(t_full, 1), "factor_s": round(t_factor, 1),
+        "cpu_baseline": {"value": round(value, 1), "unit": "ms", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} x {S} PCG iterations of the full system; per-iteration time "
+                                   f"scaled by the reference's own {iters} iterations to {args.tol:g}"},
+        "e2e": {"value": round(value, 1), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank, local, world, pg = dist_init(args)
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_gb300(args, rank, local, world, pg)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

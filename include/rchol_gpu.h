@@ -45,6 +45,9 @@ typedef struct rchol_factor_s *rchol_factor_t; /* factor G resident on the GPU  
 
 const char *rchol_gpu_last_error(void);
 const char *rchol_gpu_version(void);
+/* Number of GPU kernels the solve entry points have launched so far in this
+ * process (SpMV, triangular solves, PCG); for launch accounting. */
+int64_t rchol_gpu_launch_count(void);
 
 /* ---- ordering (host) ------------------------------------------------------
  * Nested dissection to depth log2(threads)+1 by recursive METIS vertex
@@ -130,6 +133,16 @@ int rchol_gpu_trsv_d(rchol_factor_t G, int transpose, const double *d_in, double
 /* y = A x (c++/util/pcg.cpp:130-138); device pointers. */
 int rchol_gpu_spmv_d(rchol_matrix_t A, const double *d_x, double *d_y, int64_t nrhs,
                      void *stream);
+
+/* ---- differentiation ---------------------------------------------------------
+ * No counterpart in the reference (its Python/MATLAB front ends are not
+ * differentiable).  For A(w) = sum_e w_e (u_i - u_j)(u_i - u_j)^T + diag(s),
+ * x = A^-1 b and the adjoint lambda = A^-1 dL/dx (the same G serves both
+ * solves because A is symmetric):
+ *   grad[e] = dL/dw_e = -(lambda_i - lambda_j) * (x_i - x_j)   for e = (ei[e], ej[e]).
+ * Device pointers; indices refer to the vectors as passed. */
+int rchol_gpu_edge_grad_d(int64_t nedges, const int64_t *d_ei, const int64_t *d_ej,
+                          const double *d_lambda, const double *d_x, double *d_grad, void *stream);
 
 #ifdef __cplusplus
 }

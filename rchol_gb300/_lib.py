@@ -27,6 +27,7 @@ _vp = C.c_void_p
 SIGNATURES = [
     ("rchol_gpu_last_error", C.c_char_p, []),
     ("rchol_gpu_version", C.c_char_p, []),
+    ("rchol_gpu_launch_count", _i64, []),
     ("rchol_gpu_tree_build", C.c_int, [_i64, _i64p, _i64p, C.c_int, C.POINTER(_vp)]),
     ("rchol_gpu_tree_from_partition", C.c_int, [_i64, _i64p, _i64p, _i64, C.POINTER(_vp)]),
     ("rchol_gpu_tree_size", _i64, [_vp]),
@@ -52,6 +53,7 @@ SIGNATURES = [
     ("rchol_gpu_precond_d", C.c_int, [_vp, _vp, _vp, _i64, _vp]),
     ("rchol_gpu_trsv_d", C.c_int, [_vp, C.c_int, _vp, _vp, _i64, _vp]),
     ("rchol_gpu_spmv_d", C.c_int, [_vp, _vp, _vp, _i64, _vp]),
+    ("rchol_gpu_edge_grad_d", C.c_int, [_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
 ]
 
 _lib = None

@@ -2,6 +2,7 @@
 // a status code and a thread-local message.
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -13,9 +14,11 @@ namespace rchol {
 
 namespace {
 thread_local std::string g_last_error;
-}
+std::atomic<int64_t> g_launches{0};
+}  // namespace
 
 void set_last_error(const std::string &msg) { g_last_error = msg; }
+void note_launch(int64_t count) { g_launches.fetch_add(count, std::memory_order_relaxed); }
 
 void trsv(const rchol_factor_s &F, bool upper, const double *in, double *out, int k, cudaStream_t s);
 void precond(const rchol_factor_s &F, const double *r, double *z, int k, cudaStream_t s);
@@ -23,6 +26,8 @@ void spmv_public(const rchol_matrix_s &A, const double *x, double *y, int k, cud
 void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x, int k,
                 double tol, int maxit, double *relres, int *itr, cudaStream_t s);
 int64_t plan_levels(const rchol_factor_s &F, bool upper);
+void edge_grad(int64_t m, const int64_t *ei, const int64_t *ej, const double *lam, const double *x, double *g,
+               cudaStream_t s);
 
 }  // namespace rchol
 
@@ -51,6 +56,7 @@ extern "C" {
 
 const char *rchol_gpu_last_error(void) { return g_last_error.c_str(); }
 const char *rchol_gpu_version(void) { return "rchol_gb300 0.1 (sm_103a)"; }
+int64_t rchol_gpu_launch_count(void) { return g_launches.load(); }
 
 // ---- ordering ---------------------------------------------------------------
 
@@ -133,6 +139,7 @@ int rchol_gpu_matrix_create(int64_t n, const int64_t *row_ptr, const int64_t *co
   A->ci.upload(ci32.data(), A->nnz);
   A->v.upload(A->host.v.data(), A->nnz);
   RCHOL_CUDA(cudaDeviceSynchronize());
+  build_sell(*A);
   *out = A.release();
   API_END
 }
@@ -150,6 +157,7 @@ int rchol_gpu_matrix_set_values(rchol_matrix_t A, const double *val) {
   }
   A->v.upload(A->host.v.data(), A->nnz);
   RCHOL_CUDA(cudaDeviceSynchronize());
+  build_sell(*A);
   API_END
 }
 
@@ -286,6 +294,15 @@ int rchol_gpu_trsv_d(rchol_factor_t G, int transpose, const double *d_in, double
   RCHOL_CHECK_ARG(G && d_in && d_out, "null argument");
   RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   trsv(*G, transpose != 0, d_in, d_out, (int)nrhs, as_stream(stream));
+  API_END
+}
+
+int rchol_gpu_edge_grad_d(int64_t nedges, const int64_t *d_ei, const int64_t *d_ej, const double *d_lambda,
+                          const double *d_x, double *d_grad, void *stream) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(nedges >= 0, "nedges must be nonnegative");
+  RCHOL_CHECK_ARG(nedges == 0 || (d_ei && d_ej && d_lambda && d_x && d_grad), "null argument");
+  edge_grad(nedges, d_ei, d_ej, d_lambda, d_x, d_grad, as_stream(stream));
   API_END
 }
 

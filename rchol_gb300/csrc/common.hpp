@@ -21,6 +21,8 @@ struct Error : std::runtime_error {
 };
 
 void set_last_error(const std::string &msg);
+// Counts kernel launches made by the solve path (rchol_gpu_launch_count).
+void note_launch(int64_t count = 1);
 
 #define RCHOL_CUDA(call)                                                                  \
   do {                                                                                    \
@@ -118,7 +120,16 @@ struct rchol_matrix_s {
   rchol::DevBuf<int64_t> rp;
   rchol::DevBuf<int32_t> ci;
   rchol::DevBuf<double> v;
+  // Sliced ELL copy for single right-hand-side SpMV: 32-row slices, entry j
+  // of row 32s+t at sell_off[s] + 32j + t (padding: column = row, value 0).
+  rchol::DevBuf<int64_t> sell_off;
+  rchol::DevBuf<int32_t> sell_ci;
+  rchol::DevBuf<double> sell_v;
 };
+
+namespace rchol {
+void build_sell(rchol_matrix_s &A);  // from A.host (solve.cu)
+}
 
 namespace rchol {
 struct SolvePlan;  // triangular-solve schedule, defined in solve.cu

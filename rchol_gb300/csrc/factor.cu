@@ -70,7 +70,8 @@ struct ElimArgs {
   double *diag;
   int *flags;
   uint64_t seed;
-  int emax;  // per-warp shared-memory capacity in entries
+  int emax;                  // per-warp buffer capacity in entries
+  unsigned char *gscratch;   // per-warp buffers in HBM when they exceed shared memory
 };
 
 __device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b) { return __umulhi(a, b); }
@@ -114,7 +115,8 @@ __global__ void eliminate_kernel(ElimArgs a) {
   if (warp >= a.num_nodes) return;
   const int E = a.emax;
   // per-warp layout: akey[E] aval[E] bkey[E] bval[E] cs[E]
-  unsigned char *base = smem_raw + (size_t)wib * (size_t)E * 40;
+  unsigned char *base = a.gscratch ? a.gscratch + (size_t)warp * (size_t)E * 40
+                                   : smem_raw + (size_t)wib * (size_t)E * 40;
   uint64_t *akey = reinterpret_cast<uint64_t *>(base);
   double *aval = reinterpret_cast<double *>(base + (size_t)E * 8);
   uint64_t *bkey = reinterpret_cast<uint64_t *>(base + (size_t)E * 16);
@@ -346,9 +348,16 @@ void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t
     }
   std::vector<int> initdeg(next);
   for (int64_t c = 0; c < next; ++c) initdeg[c] = (int)(ext.rp[c + 1] - ext.rp[c]);
-  // initial slab capacities: small for leaf columns, larger for separators
+  // initial slab capacities: small for leaf columns; separators receive the
+  // deferred fill of their whole subtree, more the higher they sit
   std::vector<uint32_t> cap(next);
-  for (int64_t c = 0; c < next; ++c) cap[c] = colleaf[c] ? 48u : 192u;
+  for (int64_t c = 0; c < next; ++c) {
+    if (colleaf[c]) cap[c] = 48u;
+    else if (coldepth[c] <= 1) cap[c] = 1024u;
+    else if (coldepth[c] == 2) cap[c] = 768u;
+    else if (coldepth[c] == 3) cap[c] = 512u;
+    else cap[c] = 256u;
+  }
   int64_t gcap = std::max<int64_t>(ext.nnz() * 10, 1024);
 
   cudaDeviceProp prop;
@@ -361,7 +370,7 @@ void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t
 
   DevBuf<double> diag(next);
   DevBuf<int> flags(NFLAGS);
-  for (int attempt = 0; attempt < 8; ++attempt) {
+  for (int attempt = 0; attempt < 12; ++attempt) {
     std::vector<int64_t> base(next + 1, 0);
     for (int64_t c = 0; c < next; ++c) base[c + 1] = base[c] + cap[c];
     DevBuf<uint32_t> fcnt(next), fcap(next);
@@ -412,8 +421,8 @@ void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t
       if (nb.empty()) continue;
       int emax = pow2_at_least(width);
       size_t per_warp = (size_t)emax * 40;
-      RCHOL_CHECK_ARG(per_warp <= smem_limit, "column too wide for shared memory");
-      int wpb = (int)std::min<size_t>(4, smem_limit / per_warp);
+      const bool in_smem = per_warp <= smem_limit;
+      int wpb = in_smem ? (int)std::min<size_t>(4, smem_limit / per_warp) : 1;
       keep.emplace_back(nb.size());
       keep.back().upload(nb.data(), nb.size(), s);
       keep.emplace_back(ne.size());
@@ -422,19 +431,36 @@ void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t
       args.node_end = keep.back().p;
       args.num_nodes = (int)nb.size();
       args.emax = emax;
+      DevBuf<unsigned char> wide;
+      if (!in_smem) wide.alloc(per_warp * nb.size());
+      args.gscratch = wide.p;
       int blocks = (int)((nb.size() + wpb - 1) / wpb);
-      eliminate_kernel<<<blocks, wpb * 32, per_warp * wpb, s>>>(args);
+      eliminate_kernel<<<blocks, wpb * 32, in_smem ? per_warp * wpb : 0, s>>>(args);
       RCHOL_CUDA(cudaGetLastError());
+      if (!in_smem) RCHOL_CUDA(cudaStreamSynchronize(s));  // `wide` is freed on scope exit
     }
     int hflags[NFLAGS];
     flags.download(hflags, NFLAGS, s);
     RCHOL_CUDA(cudaStreamSynchronize(s));
     if (hflags[FLAG_FILL] || hflags[FLAG_WIDTH]) {
+      // Counts past an overflow are lower bounds (truncated columns sample
+      // less fill), so grow every column of an overflowing depth to twice
+      // the largest count seen there, and overflowing columns to twice theirs.
       std::vector<uint32_t> cnt(next);
       fcnt.download(cnt.data(), next, s);
       RCHOL_CUDA(cudaStreamSynchronize(s));
-      for (int64_t c = 0; c < next; ++c)
-        if (cnt[c] >= cap[c]) cap[c] = std::max<uint32_t>(cap[c] * 2, cnt[c] + 16);
+      std::vector<uint32_t> depth_max(maxdepth + 2, 0);
+      std::vector<char> depth_over(maxdepth + 2, 0);
+      for (int64_t c = 0; c < next; ++c) {
+        int dd = colleaf[c] ? maxdepth + 1 : coldepth[c];
+        depth_max[dd] = std::max(depth_max[dd], cnt[c]);
+        if (cnt[c] >= cap[c]) depth_over[dd] = 1;
+      }
+      for (int64_t c = 0; c < next; ++c) {
+        int dd = colleaf[c] ? maxdepth + 1 : coldepth[c];
+        if (cnt[c] >= cap[c]) cap[c] = std::max<uint32_t>(cap[c] * 2, cnt[c] * 2);
+        if (depth_over[dd]) cap[c] = std::max<uint32_t>(cap[c], depth_max[dd] * 2);
+      }
       continue;
     }
     if (hflags[FLAG_GCAP]) {

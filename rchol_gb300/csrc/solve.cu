@@ -28,32 +28,11 @@
 
 #include "common.hpp"
 #include "host.hpp"
+#include "plan.hpp"
 
 namespace rchol {
 
 void exclusive_scan_i64(int64_t *d_data, int64_t n, cudaStream_t s);
-
-struct DirPlan {
-  std::vector<int> stage_ptr;   // nodes of stage s: [stage_ptr[s], stage_ptr[s+1])
-  std::vector<int> stage_maxrows;
-  DevBuf<int64_t> nb, ne;       // node row range (clipped to n)
-  DevBuf<int64_t> lvl_off;      // node k owns level entries [lvl_off[k], lvl_off[k+1])
-  DevBuf<int64_t> level_ptr;    // row offsets of each level (size = total levels + 1 per node, packed)
-  DevBuf<int32_t> rows;         // rows in per-node level order
-  DevBuf<int32_t> split;        // fwd: #leading external entries; bwd: index of first trailing external entry
-  int64_t crit_levels = 0;      // sum over stages of the deepest node
-};
-
-struct SolvePlan {
-  DirPlan fwd, bwd;
-  DevBuf<double> dinv;
-  DevBuf<float> dinv32;
-  int64_t dag_fwd = 0, dag_bwd = 0;
-  DevBuf<double> scratch;  // global fallback for nodes too large for shared memory
-  DevBuf<float> scratch32;
-  DevBuf<double> ytmp;     // intermediate of precond (FP64 path)
-  DevBuf<float> ytmp32;    // intermediate of precond (FP32 path)
-};
 
 void destroy_plan(SolvePlan *p) { delete p; }
 
@@ -198,6 +177,7 @@ void run_trsv(const rchol_factor_s &F, const SolvePlan &P, bool upper, const InT
     int64_t maxrows = D.stage_maxrows[st];
     size_t smem = (size_t)std::min<int64_t>(maxrows, a.smem_rows) * sizeof(VT) * k;
     trsv_stage_kernel<VT, InT, OutT><<<nodes, TRSV_THREADS, smem, s>>>(a, in, out);
+    note_launch();
     RCHOL_CUDA(cudaGetLastError());
   }
 }
@@ -234,17 +214,83 @@ __global__ void spmvk_kernel(int64_t n, int k, const int64_t *__restrict__ rp,
   }
 }
 
+// y = A x, sliced ELL: one thread per row, each of a warp's loads is one
+// contiguous 128/256-byte transaction.
+__global__ void __launch_bounds__(256) spmv_sell_kernel(int64_t n, const int64_t *__restrict__ off,
+                                                        const int32_t *__restrict__ ci,
+                                                        const double *__restrict__ v,
+                                                        const double *__restrict__ x, double *__restrict__ y) {
+  const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  const int64_t sl = row >> 5;
+  const int t = (int)(row & 31);
+  const int64_t o0 = off[sl], w = (off[sl + 1] - o0) >> 5;
+  double s0 = 0.0, s1 = 0.0;
+  int64_t j = 0;
+  for (; j + 1 < w; j += 2) {
+    s0 += __ldg(&v[o0 + 32 * j + t]) * __ldg(&x[__ldg(&ci[o0 + 32 * j + t])]);
+    s1 += __ldg(&v[o0 + 32 * (j + 1) + t]) * __ldg(&x[__ldg(&ci[o0 + 32 * (j + 1) + t])]);
+  }
+  if (j < w) s0 += __ldg(&v[o0 + 32 * j + t]) * __ldg(&x[__ldg(&ci[o0 + 32 * j + t])]);
+  y[row] = s0 + s1;
+}
+
 void spmv(const rchol_matrix_s &A, const double *x, double *y, int k, cudaStream_t s) {
   const int64_t n = A.n;
-  if (k == 1) {
+  if (k == 1 && A.sell_off.p) {
+    spmv_sell_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, A.sell_off.p, A.sell_ci.p, A.sell_v.p, x, y);
+    note_launch();
+  } else if (k == 1) {
     int64_t threads = n * 8;
     spmv1_kernel<8><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, A.rp.p, A.ci.p, A.v.p, x, y);
+    note_launch();
   } else {
     int64_t threads = n * 32;
     spmvk_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(n, k, A.rp.p, A.ci.p, A.v.p, x, y);
+    note_launch();
   }
   RCHOL_CUDA(cudaGetLastError());
 }
+
+}  // namespace
+
+void build_sell(rchol_matrix_s &A) {
+  const HostCsr &H = A.host;
+  const int64_t n = H.n, ns = (n + 31) / 32;
+  std::vector<int64_t> off(ns + 1, 0);
+  for (int64_t sl = 0; sl < ns; ++sl) {
+    int64_t w = 0;
+    for (int64_t r = sl * 32; r < std::min(n, sl * 32 + 32); ++r) w = std::max(w, H.rp[r + 1] - H.rp[r]);
+    off[sl + 1] = off[sl] + 32 * w;
+  }
+  std::vector<int32_t> ci(off[ns]);
+  std::vector<double> v(off[ns], 0.0);
+  parallel_for(ns, [&](int64_t s0, int64_t s1) {
+    for (int64_t sl = s0; sl < s1; ++sl) {
+      const int64_t w = (off[sl + 1] - off[sl]) / 32;
+      for (int t = 0; t < 32; ++t) {
+        const int64_t r = sl * 32 + t;
+        const int64_t len = r < n ? H.rp[r + 1] - H.rp[r] : 0;
+        for (int64_t j = 0; j < w; ++j) {
+          const int64_t o = off[sl] + 32 * j + t;
+          if (j < len) {
+            ci[o] = (int32_t)H.ci[H.rp[r] + j];
+            v[o] = H.v[H.rp[r] + j];
+          } else {
+            ci[o] = (int32_t)std::min<int64_t>(r, n - 1);
+            v[o] = 0.0;
+          }
+        }
+      }
+    }
+  }, 1 << 12);
+  A.sell_off.upload(off.data(), ns + 1);
+  A.sell_ci.upload(ci.data(), off[ns]);
+  A.sell_v.upload(v.data(), off[ns]);
+  RCHOL_CUDA(cudaDeviceSynchronize());
+}
+
+namespace {
 
 // ---- PCG --------------------------------------------------------------------------
 //
@@ -261,8 +307,8 @@ struct PcgState {
   int *any_active;
   double *partial;  // RED_BLOCKS * k * 2
   int k;
-  double tol;
-  int maxit;
+  const double *tol;  // in device memory so that a captured graph serves any call
+  const int *maxit;
 };
 
 enum RedOp { RED_DOT = 0, RED_DOT2 = 1, RED_UPDATE = 2, RED_RESID = 3 };
@@ -358,12 +404,12 @@ __global__ void finalize_kernel(PcgState st, int op, int first, double *relres) 
     st.bnorm2[r] = t0;
     st.rnorm2[r] = t0;
     st.iters[r] = 0;
-    int act = (sqrt(t0) > sqrt(t0) * st.tol) && (st.maxit > 0);
+    int act = (sqrt(t0) > sqrt(t0) * *st.tol) && (*st.maxit > 0);
     st.active[r] = act;
     if (act) atomicOr(st.any_active, 1);
   } else if (op == FIN_BETA) {  // t0 = r.z
     if (st.active[r]) {
-      st.beta[r] = first ? 0.0 : t0 / st.rz_prev[r];
+      st.beta[r] = st.iters[r] == 0 ? 0.0 : t0 / st.rz_prev[r];
       st.rz[r] = t0;
     }
   } else if (op == FIN_ALPHA) {  // t0 = p.q, t1 = p.r
@@ -378,7 +424,7 @@ __global__ void finalize_kernel(PcgState st, int op, int first, double *relres) 
       st.rz_prev[r] = st.rz[r];
       int it = st.iters[r] + 1;
       st.iters[r] = it;
-      st.active[r] = (sqrt(t0) > sqrt(st.bnorm2[r]) * st.tol) && (it < st.maxit);
+      st.active[r] = (sqrt(t0) > sqrt(st.bnorm2[r]) * *st.tol) && (it < *st.maxit);
     }
   } else {  // FIN_RESID
     relres[r] = sqrt(t0) / sqrt(st.bnorm2[r]);
@@ -392,13 +438,13 @@ __global__ void any_active_kernel(PcgState st) {
 }
 
 // p = beta p + z (p = z on the first iteration), only for active right-hand sides.
-__global__ void pupdate_kernel(int64_t nk, PcgState st, int first, double *p, const double *z) {
+__global__ void pupdate_kernel(int64_t nk, PcgState st, double *p, const double *z) {
   if (!*st.any_active) return;
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nk) return;
   int r = (int)(i % st.k);
   if (!st.active[r]) return;
-  if (first) p[i] = z[i];
+  if (st.iters[r] == 0) p[i] = z[i];
   else p[i] = st.beta[r] * p[i] + 1.0 * z[i];
 }
 
@@ -606,8 +652,10 @@ void finish_factor(rchol_factor_s &F, cudaStream_t s) {
   DevBuf<unsigned long long> cnt(n);
   RCHOL_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), s));
   transpose_count_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, F.uci.p, cnt.p);
+  note_launch();
   F.lrp.alloc(n + 1);
   i64_from_ull_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, cnt.p, F.lrp.p);
+  note_launch();
   RCHOL_CUDA(cudaGetLastError());
   exclusive_scan_i64(F.lrp.p, n, s);
   RCHOL_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), s));
@@ -616,10 +664,12 @@ void finish_factor(rchol_factor_s &F, cudaStream_t s) {
     DevBuf<double> tv(nnz);
     transpose_scatter_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(
         n, F.urp.p, F.uci.p, F.uv.p, F.lrp.p, cnt.p, tci.p, tv.p);
+    note_launch();
     F.lci.alloc(nnz);
     F.lv.alloc(nnz);
     row_sort_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(n, F.lrp.p, tci.p, tv.p, F.lci.p,
                                                                       F.lv.p);
+    note_launch();
     RCHOL_CUDA(cudaGetLastError());
     RCHOL_CUDA(cudaStreamSynchronize(s));
   }
@@ -627,7 +677,9 @@ void finish_factor(rchol_factor_s &F, cudaStream_t s) {
     F.uv32.alloc(nnz);
     F.lv32.alloc(nnz);
     to_f32_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, F.uv.p, F.uv32.p);
+    note_launch();
     to_f32_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, F.lv.p, F.lv32.p);
+    note_launch();
     RCHOL_CUDA(cudaGetLastError());
   }
   build_plan(F, s);
@@ -651,8 +703,10 @@ void build_plan(rchol_factor_s &F, cudaStream_t s) {
     if (F.precision == RCHOL_PREC_FP32) P->dinv32.alloc(n);
     diag_inverse_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
         n, F.urp.p, F.uv.p, P->dinv.p, P->dinv32.p, F.uv32.p);
+    note_launch();
     RCHOL_CUDA(cudaGetLastError());
     RCHOL_CUDA(cudaStreamSynchronize(s));
+    build_streams(F, *P, s);
   } catch (...) {
     delete P;
     throw;
@@ -675,6 +729,11 @@ void trsv(const rchol_factor_s &F, bool upper, const double *in, double *out, in
   SolvePlan &P = *F.plan;
   bool fp32 = F.precision == RCHOL_PREC_FP32;
   ensure_scratch(P, fp32, F.n * k);
+  if (k == 1) {
+    if (fp32) stream_trsv(F, P, upper, in, nullptr, out, nullptr, s);
+    else stream_trsv(F, P, upper, in, nullptr, out, nullptr, s);
+    return;
+  }
   if (fp32) run_trsv<float, double, double>(F, P, upper, in, out, k, s);
   else run_trsv<double, double, double>(F, P, upper, in, out, k, s);
 }
@@ -683,6 +742,16 @@ void precond(const rchol_factor_s &F, const double *r, double *z, int k, cudaStr
   SolvePlan &P = *F.plan;
   bool fp32 = F.precision == RCHOL_PREC_FP32;
   ensure_scratch(P, fp32, F.n * k);
+  if (k == 1) {
+    if (fp32) {
+      stream_trsv(F, P, false, r, nullptr, nullptr, P.ytmp32.p, s);
+      stream_trsv(F, P, true, nullptr, P.ytmp32.p, z, nullptr, s);
+    } else {
+      stream_trsv(F, P, false, r, nullptr, P.ytmp.p, nullptr, s);
+      stream_trsv(F, P, true, P.ytmp.p, nullptr, z, nullptr, s);
+    }
+    return;
+  }
   if (fp32) {
     run_trsv<float, double, float>(F, P, false, r, P.ytmp32.p, k, s);
     run_trsv<float, float, double>(F, P, true, P.ytmp32.p, z, k, s);
@@ -696,72 +765,181 @@ void spmv_public(const rchol_matrix_s &A, const double *x, double *y, int k, cud
   spmv(A, x, y, k, s);
 }
 
+namespace {
+// dL/dw_e = -(lambda_i - lambda_j)(x_i - x_j): the derivative of -lambda^T A(w) x
+// with respect to one edge weight.
+__global__ void edge_grad_kernel(int64_t m, const int64_t *__restrict__ ei, const int64_t *__restrict__ ej,
+                                 const double *__restrict__ lam, const double *__restrict__ x,
+                                 double *__restrict__ g) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= m) return;
+  const int64_t i = ei[e], j = ej[e];
+  g[e] = -(lam[i] - lam[j]) * (x[i] - x[j]);
+}
+}  // namespace
+
+void edge_grad(int64_t m, const int64_t *ei, const int64_t *ej, const double *lam, const double *x, double *g,
+               cudaStream_t s) {
+  if (m <= 0) return;
+  edge_grad_kernel<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(m, ei, ej, lam, x, g);
+  note_launch();
+  RCHOL_CUDA(cudaGetLastError());
+}
+
 int64_t plan_levels(const rchol_factor_s &F, bool upper) {
   return upper ? F.plan->dag_bwd : F.plan->dag_fwd;
 }
 
 // PCG for k right-hand sides (device pointers), c++/util/pcg.cpp:57-127.
+//
+// One iteration (preconditioner, r.z, p update, SpMV with p.q and p.r, x/r
+// update with ||r||^2, stopping test) is captured once per (matrix, factor, k)
+// into a CUDA graph and replayed; every kernel returns at once when no
+// right-hand side is active any more, so the host checks convergence only
+// every few iterations.  The graph runs on the workspace's own stream, joined
+// to the caller's stream with events.
+static PcgWork &pcg_workspace(const rchol_matrix_s &A, const rchol_factor_s &F, int k) {
+  SolvePlan &P = *F.plan;
+  for (auto &w : P.pcg)
+    if (w->key_rp == A.rp.p && w->key_ci == A.ci.p && w->key_v == A.v.p && w->n == A.n &&
+        w->nnz == A.nnz && w->k == k)
+      return *w;
+  if (P.pcg.size() >= 4) P.pcg.erase(P.pcg.begin());
+  auto w = std::make_unique<PcgWork>();
+  w->key_rp = A.rp.p;
+  w->key_ci = A.ci.p;
+  w->key_v = A.v.p;
+  w->n = A.n;
+  w->nnz = A.nnz;
+  w->k = k;
+  const int64_t nk = A.n * k;
+  w->r.alloc(nk);
+  w->z.alloc(nk);
+  w->p.alloc(nk);
+  w->q.alloc(nk);
+  w->x.alloc(nk);
+  w->sc.alloc(9 * (size_t)k + 2 * (size_t)RED_BLOCKS * k + 1);
+  w->ic.alloc(2 * (size_t)k + 2);
+  RCHOL_CUDA(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+  RCHOL_CUDA(cudaEventCreateWithFlags(&w->ev_in, cudaEventDisableTiming));
+  RCHOL_CUDA(cudaEventCreateWithFlags(&w->ev_out, cudaEventDisableTiming));
+  P.pcg.push_back(std::move(w));
+  return *P.pcg.back();
+}
+
+static PcgState pcg_state(PcgWork &w) {
+  const int k = w.k;
+  PcgState st;
+  double *sc = w.sc.p;
+  st.bnorm2 = sc;
+  st.rnorm2 = sc + k;
+  st.rz = sc + 2 * k;
+  st.rz_prev = sc + 3 * k;
+  st.pr = sc + 4 * k;
+  st.pq = sc + 5 * k;
+  st.alpha = sc + 6 * k;
+  st.beta = sc + 7 * k;
+  st.partial = sc + 8 * k;
+  // [8k, 8k + 2*RB*k) partial sums, then k relres slots, then tol
+  st.tol = sc + 9 * k + 2 * (size_t)RED_BLOCKS * k;
+  st.active = w.ic.p;
+  st.iters = w.ic.p + k;
+  st.any_active = w.ic.p + 2 * k;
+  st.maxit = w.ic.p + 2 * k + 1;
+  st.k = k;
+  return st;
+}
+
+static void pcg_iteration(const rchol_matrix_s &A, const rchol_factor_s &F, PcgWork &w, const PcgState &st,
+                          cudaStream_t s) {
+  const int k = w.k;
+  const int64_t n = A.n, nk = n * k;
+  const unsigned eb = (unsigned)((nk + 255) / 256);
+  precond(F, w.r.p, w.z.p, k, s);
+  reduce_kernel<RED_DOT><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, w.r.p, w.z.p, nullptr, nullptr, nullptr);
+  finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_BETA, 0, nullptr);
+  pupdate_kernel<<<eb, 256, 0, s>>>(nk, st, w.p.p, w.z.p);
+  spmv(A, w.p.p, w.q.p, k, s);
+  reduce_kernel<RED_DOT2><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, w.p.p, w.q.p, nullptr, nullptr, w.r.p);
+  finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_ALPHA, 0, nullptr);
+  reduce_kernel<RED_UPDATE><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, w.p.p, w.q.p, w.x.p, w.r.p, nullptr);
+  finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_CONV, 0, nullptr);
+  any_active_kernel<<<1, 1, 0, s>>>(st);
+  RCHOL_CUDA(cudaGetLastError());
+}
+
 void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x,
                 int k, double tol, int maxit, double *relres, int *itr, cudaStream_t s) {
+  SolvePlan &P = *F.plan;
+  std::lock_guard<std::mutex> guard(P.lock);
   const int64_t n = A.n, nk = n * k;
-  DevBuf<double> r(nk), z(nk), p(nk), q(nk);
-  DevBuf<double> sc(8 * (size_t)k + 2 * (size_t)RED_BLOCKS * k + k);
-  DevBuf<int> ic(2 * (size_t)k + 1);
-  RCHOL_CUDA(cudaMemsetAsync(sc.p, 0, sc.bytes(), s));
-  RCHOL_CUDA(cudaMemsetAsync(ic.p, 0, ic.bytes(), s));
-  PcgState st;
-  st.bnorm2 = sc.p;
-  st.rnorm2 = sc.p + k;
-  st.rz = sc.p + 2 * k;
-  st.rz_prev = sc.p + 3 * k;
-  st.pr = sc.p + 4 * k;
-  st.pq = sc.p + 5 * k;
-  st.alpha = sc.p + 6 * k;
-  st.beta = sc.p + 7 * k;
-  st.partial = sc.p + 8 * k;
-  double *d_relres = sc.p + 8 * k + 2 * (size_t)RED_BLOCKS * k;
-  st.active = ic.p;
-  st.iters = ic.p + k;
-  st.any_active = ic.p + 2 * k;
-  st.k = k;
-  st.tol = tol;
-  st.maxit = maxit;
+  const bool fp32 = F.precision == RCHOL_PREC_FP32;
+  ensure_scratch(P, fp32, nk);
+  if (fp32 ? P.acc32.n < (size_t)n : P.acc64.n < (size_t)n) {
+    if (fp32) P.acc32.alloc(n);
+    else P.acc64.alloc(n);
+  }
+  PcgWork &w = pcg_workspace(A, F, k);
+  PcgState st = pcg_state(w);
+  cudaStream_t ws = w.stream;
+  RCHOL_CUDA(cudaEventRecord(w.ev_in, s));
+  RCHOL_CUDA(cudaStreamWaitEvent(ws, w.ev_in, 0));
+  if (!w.exec) {
+    cudaGraph_t g = nullptr;
+    RCHOL_CUDA(cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal));
+    try {
+      pcg_iteration(A, F, w, st, ws);
+    } catch (...) {
+      cudaStreamEndCapture(ws, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    RCHOL_CUDA(cudaStreamEndCapture(ws, &g));
+    size_t nodes = 0;
+    RCHOL_CUDA(cudaGraphGetNodes(g, nullptr, &nodes));
+    w.graph_kernels = (int64_t)nodes;
+    cudaError_t e = cudaGraphInstantiate(&w.exec, g, 0);
+    cudaGraphDestroy(g);
+    RCHOL_CUDA(e);
+  }
+  // setup: tolerances, x = 0, r = b, ||b||^2 and the initial stopping test
+  double htol = tol;
+  int hmax = maxit;
+  RCHOL_CUDA(cudaMemsetAsync(w.sc.p, 0, w.sc.bytes(), ws));
+  RCHOL_CUDA(cudaMemsetAsync(w.ic.p, 0, w.ic.bytes(), ws));
+  RCHOL_CUDA(cudaMemcpyAsync(const_cast<double *>(st.tol), &htol, sizeof(double), cudaMemcpyHostToDevice, ws));
+  RCHOL_CUDA(cudaMemcpyAsync(const_cast<int *>(st.maxit), &hmax, sizeof(int), cudaMemcpyHostToDevice, ws));
   const unsigned eb = (unsigned)((nk + 255) / 256);
-  init_kernel<<<eb, 256, 0, s>>>(nk, b, x, r.p);
-  // ||b||^2 through the residual reduction (b - 0), which runs before any
-  // right-hand side is marked active
-  RCHOL_CUDA(cudaMemsetAsync(q.p, 0, q.bytes(), s));
-  reduce_kernel<RED_RESID><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, b, q.p, nullptr, nullptr, nullptr);
-  finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_INIT, 0, nullptr);
+  init_kernel<<<eb, 256, 0, ws>>>(nk, b, w.x.p, w.r.p);
+  RCHOL_CUDA(cudaMemsetAsync(w.q.p, 0, w.q.bytes(), ws));
+  reduce_kernel<RED_RESID><<<RED_BLOCKS, RED_THREADS, 0, ws>>>(n, st, b, w.q.p, nullptr, nullptr, nullptr);
+  finalize_kernel<<<k, RED_THREADS, 0, ws>>>(st, FIN_INIT, 0, nullptr);
+  note_launch(3);
   RCHOL_CUDA(cudaGetLastError());
   int h_any = 1;
-  for (int it = 0; it < maxit; ++it) {
-    const int first = it == 0;
-    precond(F, r.p, z.p, k, s);
-    reduce_kernel<RED_DOT><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, r.p, z.p, nullptr, nullptr, nullptr);
-    finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_BETA, first, nullptr);
-    pupdate_kernel<<<eb, 256, 0, s>>>(nk, st, first, p.p, z.p);
-    spmv(A, p.p, q.p, k, s);
-    reduce_kernel<RED_DOT2><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, p.p, q.p, nullptr, nullptr, r.p);
-    finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_ALPHA, first, nullptr);
-    reduce_kernel<RED_UPDATE><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, p.p, q.p, x, r.p, nullptr);
-    finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_CONV, first, nullptr);
-    any_active_kernel<<<1, 1, 0, s>>>(st);
-    RCHOL_CUDA(cudaGetLastError());
-    if ((it & 3) == 3 || it + 1 == maxit) {
-      RCHOL_CUDA(cudaMemcpyAsync(&h_any, st.any_active, sizeof(int), cudaMemcpyDeviceToHost, s));
-      RCHOL_CUDA(cudaStreamSynchronize(s));
-      if (!h_any) break;
+  for (int it = 0; it < maxit;) {
+    const int batch = it == 0 ? 8 : 4;
+    for (int j = 0; j < batch && it < maxit; ++j, ++it) {
+      RCHOL_CUDA(cudaGraphLaunch(w.exec, ws));
+      note_launch(w.graph_kernels);
     }
+    RCHOL_CUDA(cudaMemcpyAsync(&h_any, st.any_active, sizeof(int), cudaMemcpyDeviceToHost, ws));
+    RCHOL_CUDA(cudaStreamSynchronize(ws));
+    if (!h_any) break;
   }
-  // relres = ||A x - b|| / ||b||
-  spmv(A, x, q.p, k, s);
-  reduce_kernel<RED_RESID><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, q.p, b, nullptr, nullptr, nullptr);
-  finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_RESID, 0, d_relres);
+  // x out, relres = ||A x - b|| / ||b||
+  double *d_relres = w.sc.p + 8 * (size_t)k + 2 * (size_t)RED_BLOCKS * k;
+  spmv(A, w.x.p, w.q.p, k, ws);
+  reduce_kernel<RED_RESID><<<RED_BLOCKS, RED_THREADS, 0, ws>>>(n, st, w.q.p, b, nullptr, nullptr, nullptr);
+  finalize_kernel<<<k, RED_THREADS, 0, ws>>>(st, FIN_RESID, 0, d_relres);
+  note_launch(3);
   RCHOL_CUDA(cudaGetLastError());
-  RCHOL_CUDA(cudaMemcpyAsync(relres, d_relres, k * sizeof(double), cudaMemcpyDeviceToHost, s));
-  RCHOL_CUDA(cudaMemcpyAsync(itr, st.iters, k * sizeof(int), cudaMemcpyDeviceToHost, s));
-  RCHOL_CUDA(cudaStreamSynchronize(s));
+  RCHOL_CUDA(cudaMemcpyAsync(x, w.x.p, nk * sizeof(double), cudaMemcpyDeviceToDevice, ws));
+  RCHOL_CUDA(cudaMemcpyAsync(relres, d_relres, k * sizeof(double), cudaMemcpyDeviceToHost, ws));
+  RCHOL_CUDA(cudaMemcpyAsync(itr, st.iters, k * sizeof(int), cudaMemcpyDeviceToHost, ws));
+  RCHOL_CUDA(cudaEventRecord(w.ev_out, ws));
+  RCHOL_CUDA(cudaStreamWaitEvent(s, w.ev_out, 0));
+  RCHOL_CUDA(cudaStreamSynchronize(ws));
 }
 
 }  // namespace rchol

@@ -26,6 +26,20 @@ def test_library_exports_every_declared_symbol(built):
     assert not missing, missing
 
 
+def test_no_unresolved_internal_symbols(built):
+    """Every internal function the library calls is defined in it (lazy
+    binding would otherwise only fail at the first call, on a GPU)."""
+    import subprocess
+
+    from rchol_gb300 import _lib
+
+    out = subprocess.run(["nm", "-D", "-C", "--undefined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    bad = [ln for ln in out.splitlines() if "rchol" in ln]
+    assert not bad, bad
+    ctypes.CDLL(_lib.LIB_PATH, mode=os.RTLD_NOW)
+
+
 def test_ctypes_table_covers_header(built):
     from rchol_gb300 import _lib
 

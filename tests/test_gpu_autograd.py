@@ -1,0 +1,94 @@
+"""Gradients of x = A(w)^-1 b through the adjoint PCG (same factor) and the
+edge-gradient kernel, against a dense-solve reference gradient and FP64
+central finite differences (step 1e-6)."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def grid_edges(nx, ny):
+    idx = np.arange(nx * ny).reshape(nx, ny)
+    ei = np.concatenate([idx[:-1, :].ravel(), idx[:, :-1].ravel()])
+    ej = np.concatenate([idx[1:, :].ravel(), idx[:, 1:].ravel()])
+    return ei, ej
+
+
+def problem(nx, seed=0):
+    rng = np.random.default_rng(seed)
+    ei, ej = grid_edges(nx, nx)
+    w = 10.0 ** rng.uniform(-2.0, 2.0, len(ei))  # log-uniform in [1e-2, 1e2]
+    b = rng.standard_normal(nx * nx)
+    xt = rng.standard_normal(nx * nx)
+    return ei, ej, w, b, xt
+
+
+def test_dense_reference_gradient(cuda):
+    import torch
+
+    from rchol_gb300.autograd import LaplacianOperator, laplacian_solve
+
+    nx = 64
+    ei, ej, w0, b0, xt0 = problem(nx, seed=1)
+    op = LaplacianOperator(nx * nx, ei, ej, shift=1e-4, nt=16)
+    w = torch.tensor(w0, device=cuda, requires_grad=True)
+    b = torch.tensor(b0, device=cuda, requires_grad=True)
+    xt = torch.tensor(xt0, device=cuda)
+    x = laplacian_solve(w, b, op, tol=1e-13)
+    loss = 0.5 * ((x - xt) ** 2).sum()
+    loss.backward()
+    A = op.matrix(w0).toarray()
+    xd = np.linalg.solve(A, b0)
+    lam = np.linalg.solve(A, xd - xt0)
+    gw_ref = -(lam[ei] - lam[ej]) * (xd[ei] - xd[ej])
+    assert np.linalg.norm(x.detach().cpu().numpy() - xd) / np.linalg.norm(xd) < 1e-9
+    assert np.linalg.norm(b.grad.cpu().numpy() - lam) / np.linalg.norm(lam) < 1e-8
+    assert np.linalg.norm(w.grad.cpu().numpy() - gw_ref) / np.linalg.norm(gw_ref) < 1e-7
+
+
+def test_finite_differences_200_edges(cuda):
+    import torch
+
+    from rchol_gb300.autograd import LaplacianOperator, laplacian_solve
+
+    nx = 96
+    ei, ej, w0, b0, xt0 = problem(nx, seed=2)
+    op = LaplacianOperator(nx * nx, ei, ej, shift=1e-4, nt=32)
+    b = torch.tensor(b0, device=cuda)
+    xt = torch.tensor(xt0, device=cuda)
+
+    def loss_of(wn):
+        wt = torch.tensor(wn, device=cuda)
+        x = laplacian_solve(wt, b, op, tol=1e-14, maxit=2000)
+        return 0.5 * float(((x - xt) ** 2).sum())
+
+    w = torch.tensor(w0, device=cuda, requires_grad=True)
+    x = laplacian_solve(w, b, op, tol=1e-14, maxit=2000)
+    (0.5 * ((x - xt) ** 2).sum()).backward()
+    g = w.grad.cpu().numpy()
+    edges = np.random.default_rng(3).choice(len(ei), 200, replace=False)
+    h = 1e-6
+    fd = np.empty(len(edges))
+    for t, e in enumerate(edges):
+        wp, wm = w0.copy(), w0.copy()
+        wp[e] += h
+        wm[e] -= h
+        fd[t] = (loss_of(wp) - loss_of(wm)) / (2 * h)
+    err = np.abs(fd - g[edges]) / (np.abs(g[edges]) + 1e-6 * np.abs(g).max())
+    assert np.median(err) < 1e-5 and err.max() < 1e-2, (np.median(err), err.max())
+
+
+def test_gradcheck_small(cuda):
+    import torch
+
+    from rchol_gb300.autograd import LaplacianOperator, laplacian_solve
+
+    nx = 6
+    ei, ej, w0, b0, _ = problem(nx, seed=4)
+    w0 = 10.0 ** np.random.default_rng(5).uniform(-0.5, 0.5, len(ei))
+    op = LaplacianOperator(nx * nx, ei, ej, shift=0.1, nt=2)
+    w = torch.tensor(w0, device=cuda, requires_grad=True)
+    b = torch.tensor(b0, device=cuda, requires_grad=True)
+    f = lambda w_, b_: laplacian_solve(w_, b_, op, tol=1e-15, maxit=500)
+    assert torch.autograd.gradcheck(f, (w, b), eps=1e-6, atol=1e-6, rtol=1e-4)
