@@ -244,13 +244,16 @@ def run_gb300(args, rank, local, world, pg):
     peak, peak_kind = measured_peak_hbm()
     gbs = lambda by, ms: by / (ms * 1e-3) / 1e9
 
-    # end to end through the C ABI with host buffers
-    x_host = np.zeros(n)
+    # end to end through the C ABI with host buffers (pinned: b in, x out)
+    b_pin = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    x_pin = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    b_pin.numpy()[:] = bp
+    b_host, x_host = b_pin.numpy(), x_pin.numpy()
     rr_h = np.zeros(1)
     it_h = np.zeros(1, dtype=np.int32)
 
     def solve_host():
-        _lib.check(L.rchol_gpu_pcg(Ad.ptr, F32.ptr, _lib.pd(bp), _lib.pd(x_host), 1, args.tol, args.maxit,
+        _lib.check(L.rchol_gpu_pcg(Ad.ptr, F32.ptr, _lib.pd(b_host), _lib.pd(x_host), 1, args.tol, args.maxit,
                                    _lib.pd(rr_h), it_h.ctypes.data_as(_lib._ip)))
 
     for _ in range(args.warmup):

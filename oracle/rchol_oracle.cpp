@@ -539,6 +539,50 @@ void precond(const Csr &U, const double *r, double *z, std::vector<double> &y) {
   }
 }
 
+// The same two solves in another valid FP64 evaluation order: the forward
+// sweep in dot form over the rows of G (each row's terms summed from its last
+// column down), the backward sweep summing each row from its last column.
+// Used only to measure how far the reference PCG itself moves when nothing
+// but the rounding order changes.
+void precond_alt(const Csr &U, const Csr &L, const double *r, double *z, std::vector<double> &y) {
+  int64_t n = U.n;
+  y.assign(n, 0.0);
+  for (int64_t i = 0; i < n; ++i) {
+    double acc = 0.0, d = 0.0;
+    for (uint64_t k = L.rp[i + 1]; k-- > L.rp[i];) {
+      if (L.ci[k] == (uint64_t)i) d = L.v[k];
+      else if (L.ci[k] < (uint64_t)i) acc += L.v[k] * y[L.ci[k]];
+    }
+    y[i] = (r[i] - acc) / d;
+  }
+  for (int64_t i = n - 1; i >= 0; --i) {
+    double acc = 0.0, d = 0.0;
+    for (uint64_t k = U.rp[i + 1]; k-- > U.rp[i];) {
+      if (U.ci[k] == (uint64_t)i) d = U.v[k];
+      else if (U.ci[k] > (uint64_t)i) acc += U.v[k] * z[U.ci[k]];
+    }
+    z[i] = (y[i] - acc) / d;
+  }
+}
+
+Csr transpose(const Csr &U) {
+  Csr L;
+  L.n = U.n;
+  L.rp.assign(U.n + 1, 0);
+  for (uint64_t k = 0; k < U.rp[U.n]; ++k) ++L.rp[U.ci[k] + 1];
+  for (int64_t i = 0; i < U.n; ++i) L.rp[i + 1] += L.rp[i];
+  L.ci.resize(U.rp[U.n]);
+  L.v.resize(U.rp[U.n]);
+  std::vector<uint64_t> cur(L.rp.begin(), L.rp.end() - 1);
+  for (int64_t i = 0; i < U.n; ++i)
+    for (uint64_t k = U.rp[i]; k < U.rp[i + 1]; ++k) {
+      const uint64_t w = cur[U.ci[k]]++;
+      L.ci[w] = (uint64_t)i;
+      L.v[w] = U.v[k];
+    }
+  return L;
+}
+
 void spmv(const Csr &A, const double *x, double *y, int threads) {
 #pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
   for (int64_t i = 0; i < A.n; ++i) {
@@ -724,20 +768,28 @@ int oracle_spmv(int64_t n, const uint64_t *rp, const uint64_t *ci, const double 
 
 // c++/util/pcg.cpp:57-127.  With threads == 1 the arithmetic follows the
 // serial MKL stand-in exactly; threads > 1 parallelises SpMV (same per-row
-// order) and the dot products (different summation order).  If hist is
-// non-null, ||r_k|| / ||b|| after each iteration k is stored in hist[k].
+// order) and the dot products (different summation order); threads < 0 uses
+// |threads| threads and also the other evaluation order of the triangular
+// solves (precond_alt).  The last two only measure rounding sensitivity.  If
+// hist is non-null, ||r_k|| / ||b|| after each iteration k is stored in
+// hist[k].
 int oracle_pcg(int64_t n, const uint64_t *rp, const uint64_t *ci, const double *v,
                const double *b, double tol, int maxit, const uint64_t *grp,
                const uint64_t *gci, const double *gv, int threads, double *x,
                double *relres, int *itr, double *hist) {
   Csr A = make(n, rp, ci, v);
   Csr U = make(n, grp, gci, gv);
+  const bool alt = threads < 0;
+  threads = std::abs(threads);
+  Csr L;
+  if (alt) L = transpose(U);
   std::vector<double> r(b, b + n), pr(n, 0.0), pz(n, 0.0), p(n, 0.0), z(n, 0.0), q(n, 0.0), y;
   std::fill(x, x + n, 0.0);
   double nb = std::sqrt(dot(n, b, b, threads));
   int it = 0;
   while (std::sqrt(dot(n, r.data(), r.data(), threads)) > nb * tol && it < maxit) {
-    precond(U, r.data(), z.data(), y);
+    if (alt) precond_alt(U, L, r.data(), z.data(), y);
+    else precond(U, r.data(), z.data(), y);
     if (it == 0) {
       p = z;
     } else {

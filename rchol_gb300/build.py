@@ -51,9 +51,12 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
     headers = glob.glob(os.path.join(CSRC, "*.hpp")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
     jobs = []
+    checks = bool(os.environ.get("RCHOL_DEVICE_CHECKS"))
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cu"))):
-        obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+        obj = os.path.join(OBJ, os.path.basename(src) + (".chk.o" if checks else ".o"))
         cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *inc, "-c", src, "-o", obj]
+        if os.environ.get("RCHOL_DEVICE_CHECKS"):  # diagnostic build: device-side bounds checks
+            cmd.insert(1, "-DRCHOL_DEVICE_CHECKS")
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")
         jobs.append((obj, cmd, [src, *headers]))
@@ -68,8 +71,13 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         for out in ex.map(lambda j: _run(j[1]), todo):
             logs.append(out)
     objs = [j[0] for j in jobs]
-    if todo or not os.path.exists(LIB):
+    stamp_path = os.path.join(OBJ, "link.stamp")
+    stamp = "\n".join(objs)
+    old = open(stamp_path).read() if os.path.exists(stamp_path) else ""
+    if todo or not os.path.exists(LIB) or old != stamp:
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, metis_archive(), "-lpthread"])
+        with open(stamp_path, "w") as f:
+            f.write(stamp)
     log = "\n".join(l for l in logs if l.strip())
     if verbose and log:
         print(log, file=sys.stderr)

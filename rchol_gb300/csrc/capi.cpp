@@ -15,6 +15,7 @@ namespace rchol {
 namespace {
 thread_local std::string g_last_error;
 std::atomic<int64_t> g_launches{0};
+std::atomic<uint64_t> g_matrix_uid{0};
 }  // namespace
 
 void set_last_error(const std::string &msg) { g_last_error = msg; }
@@ -25,6 +26,8 @@ void precond(const rchol_factor_s &F, const double *r, double *z, int k, cudaStr
 void spmv_public(const rchol_matrix_s &A, const double *x, double *y, int k, cudaStream_t s);
 void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x, int k,
                 double tol, int maxit, double *relres, int *itr, cudaStream_t s);
+void pcg_host(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x, int k,
+              double tol, int maxit, double *relres, int *itr);
 int64_t plan_levels(const rchol_factor_s &F, bool upper);
 void edge_grad(int64_t m, const int64_t *ei, const int64_t *ej, const double *lam, const double *x, double *g,
                cudaStream_t s);
@@ -119,6 +122,7 @@ int rchol_gpu_matrix_create(int64_t n, const int64_t *row_ptr, const int64_t *co
   validate_csr(n, row_ptr, col_idx);
   RCHOL_CHECK_ARG(!tree || tree->n == n, "tree and matrix sizes differ");
   std::unique_ptr<rchol_matrix_s> A(new rchol_matrix_s());
+  A->uid = ++g_matrix_uid;
   A->n = n;
   A->nnz = row_ptr[n];
   if (tree) {
@@ -270,12 +274,7 @@ int rchol_gpu_pcg(rchol_matrix_t A, rchol_factor_t G, const double *b, double *x
   RCHOL_CHECK_ARG(A && G && b && x && relres && itr, "null argument");
   RCHOL_CHECK_ARG(A->n == G->n, "matrix and factor sizes differ");
   RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
-  const int64_t nk = A->n * nrhs;
-  DevBuf<double> db(nk), dx(nk);
-  db.upload(b, nk);
-  pcg_device(*A, *G, db.p, dx.p, (int)nrhs, tol, maxit, relres, itr, 0);
-  dx.download(x, nk);
-  RCHOL_CUDA(cudaDeviceSynchronize());
+  pcg_host(*A, *G, b, x, (int)nrhs, tol, maxit, relres, itr);
   API_END
 }
 

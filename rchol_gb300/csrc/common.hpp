@@ -111,6 +111,7 @@ struct rchol_tree_s {
 };
 
 struct rchol_matrix_s {
+  uint64_t uid = 0;  // unique per created matrix (keys cached solve workspaces)
   int64_t n = 0;
   int64_t nnz = 0;
   bool permuted = false;

@@ -18,28 +18,32 @@ namespace rchol {
 //     ext_rp / ext_ci / ext_v, consumed by the prologue;
 //   * in an earlier block of the piece: kept sparse in the block's record;
 //   * inside the block: folded into the exact inverse of the block's 32x32
-//     triangle, stored dense.
-// Block record (16-byte aligned, in processing order):
-//   u32 nrows, nent, row0 (piece-local first row), col_bytes
-//   u32 ent_off[33]                     lane r owns entries [ent_off[r], ent_off[r+1])
-//   u16|u32 ent_col[nent]               piece-local columns
-//   VT  ent_val[nent]
-//   VT  minv[32*32]                     minv[c*32 + r] = (T^-1)_{r,c}
+//     triangle, stored packed by columns (528 values).
+// Two record formats exist (trsv.cu documents both): the warp format, where
+// one warp solves a piece and lane r sums row r's sparse entries, and the
+// team format, where a thread block solves a piece, its helper warps sum the
+// entries from blocks older than the previous one in balanced chunks, and
+// one warp adds the previous block's entries and applies the inverse.
 struct NodeDesc {
   int64_t begin;    // first row of the piece
   int32_t rows;
   int32_t nblocks;
   int64_t blk0;     // offsets of its blocks: blk_off[blk0 .. blk0 + nblocks]
   int32_t maxrec;   // largest block record (bytes)
-  int32_t wide;     // ent_col is u32 (piece larger than 65535 rows)
+  int32_t wide;     // column indices are u32 (piece larger than 65535 rows)
+  int32_t maxchunk; // team format: most chunks of one block
+  int32_t pad_;
 };
 
 struct StreamDir {
   std::vector<int> stage_ptr;        // pieces of stage s: [stage_ptr[s], stage_ptr[s+1])
-  std::vector<int> stage_split;      // stage uses the multi-block external kernel
   std::vector<int> stage_rows;       // largest piece of the stage (rows)
   std::vector<int> stage_maxrec;     // largest block record of the stage (bytes)
   std::vector<int64_t> stage_row_ptr;  // rows of split stages: srows[stage_row_ptr[s] ..]
+  std::vector<int> stage_team;       // 1: team format (a thread block per piece)
+  std::vector<int> stage_chunks;     // team format: most chunks of one block in the stage
+  std::vector<int> stage_ext_lanes;  // lanes per row of the external prologue (1, 4, 8 or 32)
+  int team_warps = 8;                // warps of a team (1 solver + helpers)
   DevBuf<int32_t> srows;
   DevBuf<NodeDesc> nodes;
   DevBuf<int64_t> ext_rp;
@@ -67,10 +71,11 @@ struct DirPlan {
 // Workspace and captured CUDA graph of one PCG iteration for a given matrix
 // and number of right-hand sides (solve.cu).
 struct PcgWork {
-  const void *key_rp = nullptr, *key_ci = nullptr, *key_v = nullptr;
+  uint64_t key_uid = 0;  // the matrix the captured iteration reads
   int64_t n = 0, nnz = 0;
   int k = 0;
   DevBuf<double> r, z, p, q, x, sc;
+  DevBuf<double> hb, hx;  // staging of the host-buffer entry point
   DevBuf<int> ic;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;

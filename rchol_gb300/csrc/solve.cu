@@ -715,18 +715,27 @@ void build_plan(rchol_factor_s &F, cudaStream_t s) {
   F.plan = P;
 }
 
+// Grows the plan's temporaries.  Growing frees buffers that captured PCG
+// graphs point to, so every cached graph of this factor is dropped with them
+// (a replay would otherwise read and write freed memory).  Callers hold P.lock.
 static void ensure_scratch(SolvePlan &P, bool fp32, int64_t count) {
+  bool grew = false;
   if (fp32) {
-    if (P.scratch32.n < (size_t)count) P.scratch32.alloc(count);
-    if (P.ytmp32.n < (size_t)count) P.ytmp32.alloc(count);
+    if (P.scratch32.n < (size_t)count) P.scratch32.alloc(count), grew = true;
+    if (P.ytmp32.n < (size_t)count) P.ytmp32.alloc(count), grew = true;
   } else {
-    if (P.scratch.n < (size_t)count) P.scratch.alloc(count);
-    if (P.ytmp.n < (size_t)count) P.ytmp.alloc(count);
+    if (P.scratch.n < (size_t)count) P.scratch.alloc(count), grew = true;
+    if (P.ytmp.n < (size_t)count) P.ytmp.alloc(count), grew = true;
   }
+  if (grew) P.pcg.clear();
 }
+
+// The preconditioner with the plan's buffers already sized (inside PCG).
+static void precond_ready(const rchol_factor_s &F, const double *r, double *z, int k, cudaStream_t s);
 
 void trsv(const rchol_factor_s &F, bool upper, const double *in, double *out, int k, cudaStream_t s) {
   SolvePlan &P = *F.plan;
+  std::lock_guard<std::mutex> guard(P.lock);
   bool fp32 = F.precision == RCHOL_PREC_FP32;
   ensure_scratch(P, fp32, F.n * k);
   if (k == 1) {
@@ -740,8 +749,14 @@ void trsv(const rchol_factor_s &F, bool upper, const double *in, double *out, in
 
 void precond(const rchol_factor_s &F, const double *r, double *z, int k, cudaStream_t s) {
   SolvePlan &P = *F.plan;
-  bool fp32 = F.precision == RCHOL_PREC_FP32;
-  ensure_scratch(P, fp32, F.n * k);
+  std::lock_guard<std::mutex> guard(P.lock);
+  ensure_scratch(P, F.precision == RCHOL_PREC_FP32, F.n * k);
+  precond_ready(F, r, z, k, s);
+}
+
+static void precond_ready(const rchol_factor_s &F, const double *r, double *z, int k, cudaStream_t s) {
+  SolvePlan &P = *F.plan;
+  const bool fp32 = F.precision == RCHOL_PREC_FP32;
   if (k == 1) {
     if (fp32) {
       stream_trsv(F, P, false, r, nullptr, nullptr, P.ytmp32.p, s);
@@ -801,14 +816,11 @@ int64_t plan_levels(const rchol_factor_s &F, bool upper) {
 static PcgWork &pcg_workspace(const rchol_matrix_s &A, const rchol_factor_s &F, int k) {
   SolvePlan &P = *F.plan;
   for (auto &w : P.pcg)
-    if (w->key_rp == A.rp.p && w->key_ci == A.ci.p && w->key_v == A.v.p && w->n == A.n &&
-        w->nnz == A.nnz && w->k == k)
+    if (w->key_uid == A.uid && w->n == A.n && w->nnz == A.nnz && w->k == k)
       return *w;
   if (P.pcg.size() >= 4) P.pcg.erase(P.pcg.begin());
   auto w = std::make_unique<PcgWork>();
-  w->key_rp = A.rp.p;
-  w->key_ci = A.ci.p;
-  w->key_v = A.v.p;
+  w->key_uid = A.uid;
   w->n = A.n;
   w->nnz = A.nnz;
   w->k = k;
@@ -855,7 +867,7 @@ static void pcg_iteration(const rchol_matrix_s &A, const rchol_factor_s &F, PcgW
   const int k = w.k;
   const int64_t n = A.n, nk = n * k;
   const unsigned eb = (unsigned)((nk + 255) / 256);
-  precond(F, w.r.p, w.z.p, k, s);
+  precond_ready(F, w.r.p, w.z.p, k, s);
   reduce_kernel<RED_DOT><<<RED_BLOCKS, RED_THREADS, 0, s>>>(n, st, w.r.p, w.z.p, nullptr, nullptr, nullptr);
   finalize_kernel<<<k, RED_THREADS, 0, s>>>(st, FIN_BETA, 0, nullptr);
   pupdate_kernel<<<eb, 256, 0, s>>>(nk, st, w.p.p, w.z.p);
@@ -868,8 +880,11 @@ static void pcg_iteration(const rchol_matrix_s &A, const rchol_factor_s &F, PcgW
   RCHOL_CUDA(cudaGetLastError());
 }
 
-void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x,
-                int k, double tol, int maxit, double *relres, int *itr, cudaStream_t s) {
+// b_host / x_host: the host-buffer entry point (b copied in and x copied out
+// on the workspace stream, through device staging kept with the workspace).
+static void pcg_impl(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x,
+                     const double *b_host, double *x_host, int k, double tol, int maxit, double *relres,
+                     int *itr, cudaStream_t s) {
   SolvePlan &P = *F.plan;
   std::lock_guard<std::mutex> guard(P.lock);
   const int64_t n = A.n, nk = n * k;
@@ -884,6 +899,13 @@ void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *
   cudaStream_t ws = w.stream;
   RCHOL_CUDA(cudaEventRecord(w.ev_in, s));
   RCHOL_CUDA(cudaStreamWaitEvent(ws, w.ev_in, 0));
+  if (b_host) {
+    if (w.hb.n < (size_t)nk) w.hb.alloc(nk);
+    if (w.hx.n < (size_t)nk) w.hx.alloc(nk);
+    RCHOL_CUDA(cudaMemcpyAsync(w.hb.p, b_host, nk * sizeof(double), cudaMemcpyHostToDevice, ws));
+    b = w.hb.p;
+    x = w.hx.p;
+  }
   if (!w.exec) {
     cudaGraph_t g = nullptr;
     RCHOL_CUDA(cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal));
@@ -934,12 +956,23 @@ void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *
   finalize_kernel<<<k, RED_THREADS, 0, ws>>>(st, FIN_RESID, 0, d_relres);
   note_launch(3);
   RCHOL_CUDA(cudaGetLastError());
-  RCHOL_CUDA(cudaMemcpyAsync(x, w.x.p, nk * sizeof(double), cudaMemcpyDeviceToDevice, ws));
+  if (x_host) RCHOL_CUDA(cudaMemcpyAsync(x_host, w.x.p, nk * sizeof(double), cudaMemcpyDeviceToHost, ws));
+  else RCHOL_CUDA(cudaMemcpyAsync(x, w.x.p, nk * sizeof(double), cudaMemcpyDeviceToDevice, ws));
   RCHOL_CUDA(cudaMemcpyAsync(relres, d_relres, k * sizeof(double), cudaMemcpyDeviceToHost, ws));
   RCHOL_CUDA(cudaMemcpyAsync(itr, st.iters, k * sizeof(int), cudaMemcpyDeviceToHost, ws));
   RCHOL_CUDA(cudaEventRecord(w.ev_out, ws));
   RCHOL_CUDA(cudaStreamWaitEvent(s, w.ev_out, 0));
   RCHOL_CUDA(cudaStreamSynchronize(ws));
+}
+
+void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x, int k, double tol,
+                int maxit, double *relres, int *itr, cudaStream_t s) {
+  pcg_impl(A, F, b, x, nullptr, nullptr, k, tol, maxit, relres, itr, s);
+}
+
+void pcg_host(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x, int k, double tol,
+              int maxit, double *relres, int *itr) {
+  pcg_impl(A, F, nullptr, nullptr, b, x, k, tol, maxit, relres, itr, 0);
 }
 
 }  // namespace rchol

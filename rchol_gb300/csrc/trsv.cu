@@ -37,9 +37,16 @@ namespace rchol {
 
 namespace {
 
-constexpr int BS = 32;  // rows per block
+constexpr int BS = 32;                  // rows per block
+constexpr int TRI = BS * (BS + 1) / 2;  // stored entries of a block's triangular inverse
 
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
+
+// Column c of a block inverse is stored contiguously: rows c..31 for a lower
+// (forward) inverse, rows 0..c for an upper (backward) one.
+__host__ __device__ inline int tri_col_off(int c, bool upper) {
+  return upper ? c * (c + 1) / 2 : c * BS - c * (c - 1) / 2;
+}
 
 // ---- host: one piece -----------------------------------------------------------
 
@@ -113,7 +120,7 @@ void build_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
     invert_block(T, upper, X);
     // record layout
     const size_t o_off = 16, o_col = o_off + al16(4 * (BS + 1)), o_val = o_col + al16(csz * nent),
-                 o_min = o_val + al16(vsz * nent), len = o_min + al16(vsz * BS * BS);
+                 o_min = o_val + al16(vsz * nent), len = o_min + al16(vsz * TRI);
     const size_t base = P.bytes.size();
     P.bytes.resize(base + len, 0);
     unsigned char *p = P.bytes.data() + base;
@@ -138,18 +145,166 @@ void build_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
           std::memcpy(p + o_val + 4 * w, &f, 4);
         }
       }
-    for (int c = 0; c < BS; ++c)
-      for (int r = 0; r < BS; ++r) {
+    for (int c = 0; c < BS; ++c) {
+      const int r_lo = upper ? 0 : c, r_hi = upper ? c : BS - 1;
+      for (int r = r_lo; r <= r_hi; ++r) {
         const double m = (r < nr && c < nr) ? X[r][c] : 0.0;
-        if (vsz == 8) std::memcpy(p + o_min + 8 * (c * BS + r), &m, 8);
+        const size_t at = (size_t)tri_col_off(c, upper) + (size_t)(r - r_lo);
+        if (vsz == 8) std::memcpy(p + o_min + 8 * at, &m, 8);
         else {
           float f = (float)m;
-          std::memcpy(p + o_min + 4 * (c * BS + r), &f, 4);
+          std::memcpy(p + o_min + 4 * at, &f, 4);
         }
       }
+    }
     P.offs.push_back((int64_t)P.bytes.size());
     P.maxrec = std::max<int32_t>(P.maxrec, (int32_t)len);
     P.sparse += nent;
+  }
+}
+
+// Team format.  A thread block of W warps solves the piece: warp 0 (the
+// solver) retires one block per step, while the W-1 helper warps sum, for the
+// block after it, the entries whose columns lie in blocks older than the one
+// being solved ("far" entries), in chunks of near-equal length.  The solver
+// then only adds the previous block's entries ("near") and the chunk sums of
+// its row before applying the inverse.  Record (16-byte aligned sections):
+//   u32 hdr[8]   nrows, row0, prev_row0, nnear, nchunk, nfar, col_bytes, 0
+//   u16 near_off[33]       lane r's near entries [near_off[r], near_off[r+1])
+//   u8  near_col[nnear]    column inside the previous block (0..31)
+//   VT  near_val[nnear]
+//   u16 chunk_row[33]      row r's chunks [chunk_row[r], chunk_row[r+1])
+//   u32 chunk_beg[nchunk+1] chunk c = far entries [chunk_beg[c], chunk_beg[c+1])
+//   u16|u32 far_col[nfar]  piece-local columns
+//   VT  far_val[nfar]
+//   VT  minv[528]          as in the warp format
+struct TeamLayout {
+  size_t o_noff, o_ncol, o_nval, o_crow, o_cbeg, o_fcol, o_fval, o_min, len;
+};
+
+__host__ __device__ inline TeamLayout team_layout(uint32_t nnear, uint32_t nchunk, uint32_t nfar, uint32_t csz,
+                                                  uint32_t vsz) {
+  TeamLayout L;
+  L.o_noff = 32;
+  L.o_ncol = L.o_noff + al16(2 * (BS + 1));
+  L.o_nval = L.o_ncol + al16(nnear);
+  L.o_crow = L.o_nval + al16((size_t)vsz * nnear);
+  L.o_cbeg = L.o_crow + al16(2 * (BS + 1));
+  L.o_fcol = L.o_cbeg + al16(4 * ((size_t)nchunk + 1));
+  L.o_fval = L.o_fcol + al16((size_t)csz * nfar);
+  L.o_min = L.o_fval + al16((size_t)vsz * nfar);
+  L.len = L.o_min + al16((size_t)vsz * TRI);
+  return L;
+}
+
+// Upper bound of a team record whose block has `cnt` entries in earlier
+// blocks of its piece (near and far entries together), for helpers of
+// `helper_threads` threads.
+inline size_t team_record_bound(size_t cnt, size_t helper_threads, size_t vsz, size_t csz) {
+  const size_t chunks = std::min(cnt, helper_threads + BS);
+  return 32 + 2 * al16(2 * (BS + 1)) + al16(std::min<size_t>(cnt, BS * BS)) + al16(4 * (chunks + 1)) +
+         al16(csz * cnt) + vsz * cnt + 32 + al16(vsz * TRI);
+}
+
+void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, const std::vector<double> &v,
+                      int64_t b, int64_t e, bool upper, size_t vsz, int helper_threads, PieceBuild &P,
+                      int32_t &maxchunk) {
+  const int64_t R = e - b, nb = (R + BS - 1) / BS;
+  const uint32_t csz = R > 65535 ? 4 : 2;
+  P.offs.assign(1, 0);
+  P.bytes.clear();
+  maxchunk = 0;
+  double T[BS][BS], X[BS][BS];
+  std::vector<std::pair<uint32_t, double>> nearl[BS], farl[BS];
+  for (int64_t s = 0; s < nb; ++s) {
+    const int64_t bi = upper ? nb - 1 - s : s;
+    const int64_t row0 = bi * BS;
+    const int nr = (int)std::min<int64_t>(BS, R - row0);
+    const int64_t pbi = s == 0 ? -1 : (upper ? bi + 1 : bi - 1);  // previous block, processing order
+    const int64_t prow0 = pbi < 0 ? 0 : pbi * BS;
+    for (int r = 0; r < BS; ++r) {
+      for (int c = 0; c < BS; ++c) T[r][c] = 0.0;
+      T[r][r] = 1.0;
+      nearl[r].clear();
+      farl[r].clear();
+    }
+    uint32_t nnear = 0, nfar = 0;
+    for (int r = 0; r < nr; ++r) {
+      const int64_t i = b + row0 + r;
+      for (int64_t q = rp[i]; q < rp[i + 1]; ++q) {
+        const int64_t c = ci[q];
+        if (c < b || c >= e) continue;  // external
+        const int64_t lc = c - b, cb = lc / BS;
+        if (cb == bi) {
+          T[r][lc - row0] = v[q];
+        } else if (cb == pbi) {
+          nearl[r].push_back({(uint32_t)(lc - prow0), v[q]});
+          ++nnear;
+        } else {
+          farl[r].push_back({(uint32_t)lc, v[q]});
+          ++nfar;
+        }
+      }
+    }
+    invert_block(T, upper, X);
+    // balanced chunks over the helper threads; a chunk never spans two rows
+    const uint32_t target = std::max<uint32_t>(4, (nfar + helper_threads - 1) / std::max(1, helper_threads));
+    uint16_t crow[BS + 1];
+    std::vector<uint32_t> cbeg(1, 0);
+    crow[0] = 0;
+    for (int r = 0; r < BS; ++r) {
+      const uint32_t m = (uint32_t)farl[r].size();
+      const uint32_t nc = (m + target - 1) / target, start = cbeg.back();
+      for (uint32_t j = 1; j <= nc; ++j) cbeg.push_back(start + (uint32_t)(j * (uint64_t)m / nc));
+      crow[r + 1] = (uint16_t)(cbeg.size() - 1);
+    }
+    const uint32_t nchunk = (uint32_t)cbeg.size() - 1;
+    maxchunk = std::max<int32_t>(maxchunk, (int32_t)nchunk);
+    const TeamLayout L = team_layout(nnear, nchunk, nfar, csz, (uint32_t)vsz);
+    const size_t base = P.bytes.size();
+    P.bytes.resize(base + L.len, 0);
+    unsigned char *p = P.bytes.data() + base;
+    const uint32_t hdr[8] = {(uint32_t)nr, (uint32_t)row0, (uint32_t)prow0, nnear, nchunk, nfar, csz, 0};
+    std::memcpy(p, hdr, sizeof(hdr));
+    auto put_val = [&](size_t off, size_t idx, double x) {
+      if (vsz == 8) std::memcpy(p + off + 8 * idx, &x, 8);
+      else {
+        const float f = (float)x;
+        std::memcpy(p + off + 4 * idx, &f, 4);
+      }
+    };
+    uint16_t noff[BS + 1];
+    noff[0] = 0;
+    size_t w = 0, wf = 0;
+    for (int r = 0; r < BS; ++r) {
+      for (auto &en : nearl[r]) {
+        p[L.o_ncol + w] = (unsigned char)en.first;
+        put_val(L.o_nval, w, en.second);
+        ++w;
+      }
+      noff[r + 1] = (uint16_t)w;
+      for (auto &en : farl[r]) {
+        if (csz == 2) {
+          const uint16_t c16 = (uint16_t)en.first;
+          std::memcpy(p + L.o_fcol + 2 * wf, &c16, 2);
+        } else {
+          std::memcpy(p + L.o_fcol + 4 * wf, &en.first, 4);
+        }
+        put_val(L.o_fval, wf, en.second);
+        ++wf;
+      }
+    }
+    std::memcpy(p + L.o_noff, noff, sizeof(noff));
+    std::memcpy(p + L.o_crow, crow, sizeof(crow));
+    std::memcpy(p + L.o_cbeg, cbeg.data(), 4 * cbeg.size());
+    for (int c = 0; c < BS; ++c) {
+      const int r_lo = upper ? 0 : c, r_hi = upper ? c : BS - 1;
+      for (int r = r_lo; r <= r_hi; ++r)
+        put_val(L.o_min, (size_t)tri_col_off(c, upper) + (size_t)(r - r_lo), (r < nr && c < nr) ? X[r][c] : 0.0);
+    }
+    P.offs.push_back((int64_t)P.bytes.size());
+    P.maxrec = std::max<int32_t>(P.maxrec, (int32_t)L.len);
+    P.sparse += nnear + nfar;
   }
 }
 
@@ -165,6 +320,18 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+#ifdef RCHOL_DEVICE_CHECKS
+// Diagnostic build only: bounds checks report the first violations and skip
+// the access (uniform conditions make the whole warp leave).
+__device__ int64_t dbg_n;
+__device__ unsigned dbg_count;
+__device__ void dbg_report(const char *what, int64_t v, int64_t lim) {
+  if (atomicAdd(&dbg_count, 1u) < 16u)
+    printf("[rchol check] %s: %lld (limit %lld) block %d thread %d\n", what, (long long)v, (long long)lim,
+           (int)blockIdx.x, (int)threadIdx.x);
+}
+#endif
+
 // acc_i = rhs_i - sum over row i's entries outside its piece.
 template <typename VT, typename InT, typename OutT>
 __global__ void __launch_bounds__(256) ext_kernel(const int32_t *__restrict__ rows, int64_t nrows,
@@ -174,9 +341,22 @@ __global__ void __launch_bounds__(256) ext_kernel(const int32_t *__restrict__ ro
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nrows) return;
   const int64_t i = rows[t];
+#ifdef RCHOL_DEVICE_CHECKS
+  if (i < 0 || i >= dbg_n) {
+    dbg_report("ext row", i, dbg_n);
+    return;
+  }
+#endif
   const int64_t q0 = ext_rp[i], q1 = ext_rp[i + 1];
   VT s0 = 0, s1 = 0;
   int64_t q = q0;
+#ifdef RCHOL_DEVICE_CHECKS
+  for (int64_t qq = q0; qq < q1; ++qq)
+    if (ext_ci[qq] < 0 || ext_ci[qq] >= dbg_n) {
+      dbg_report("ext col", ext_ci[qq], dbg_n);
+      return;
+    }
+#endif
   for (; q + 1 < q1; q += 2) {
     s0 += ext_v[q] * (VT)out[ext_ci[q]];
     s1 += ext_v[q + 1] * (VT)out[ext_ci[q + 1]];
@@ -191,13 +371,15 @@ struct BlockArgs {
   int node0, node1;     // pieces of this stage
   int wpb;              // warps (pieces) per thread block
   int bufbytes;         // per-buffer bytes (16-aligned)
+  int nbuf;             // block records in flight per warp (ring of buffers), 2..6
   int per_warp;         // shared-memory bytes per warp
+  bool upper;           // backward solve: upper-triangular block inverses
   const unsigned char *blocks;
   const int64_t *blk_off;
   const VT *acc;
 };
 
-template <typename VT, typename OutT>
+template <typename VT, typename OutT, bool UPPER>
 __global__ void __launch_bounds__(128) block_kernel(BlockArgs<VT> a, OutT *out) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -205,26 +387,51 @@ __global__ void __launch_bounds__(128) block_kernel(BlockArgs<VT> a, OutT *out) 
   if (piece >= a.node1) return;  // the whole warp leaves
   const NodeDesc nd = a.nodes[piece];
   unsigned char *base = smem + (size_t)w * a.per_warp;
-  unsigned char *buf0 = base, *buf1 = base + a.bufbytes;
-  VT *xs = reinterpret_cast<VT *>(base + 2 * (size_t)a.bufbytes);
+  const int nbuf = a.nbuf;
+  VT *xs = reinterpret_cast<VT *>(base + (size_t)nbuf * a.bufbytes);
   const unsigned char *src = a.blocks;
   const int64_t *boff = a.blk_off + nd.blk0;
 
-  auto load = [&](int k, unsigned char *dst) {
-    const int64_t o0 = boff[k], len = boff[k + 1] - o0;
+  // ring of nbuf block buffers; block k lives in slot k % nbuf
+  auto load = [&](int k) {
+    unsigned char *dst = base + (size_t)(k % nbuf) * a.bufbytes;
+    const int64_t o0 = boff[k];
+    int64_t len = boff[k + 1] - o0;
+#ifdef RCHOL_DEVICE_CHECKS
+    if (len < 0 || len > a.bufbytes || (o0 & 15)) {
+      if (lane == 0) dbg_report("block record length", len, a.bufbytes);
+      len = 0;
+    }
+#endif
     for (int64_t o = lane * 16; o < len; o += 32 * 16) cp_async16(dst + o, src + o0 + o);
     cp_async_commit();
   };
-  if (nd.nblocks > 0) load(0, buf0);
-  if (nd.nblocks > 1) load(1, buf1);
+#ifdef RCHOL_DEVICE_CHECKS
+  if ((int64_t)nbuf * a.bufbytes + (int64_t)nd.rows * (int64_t)sizeof(VT) > a.per_warp ||
+      nd.begin < 0 || nd.begin + nd.rows > dbg_n) {
+    if (lane == 0) dbg_report("piece layout (rows)", nd.rows, a.per_warp);
+    return;
+  }
+#endif
+  for (int k = 0; k < nbuf - 1 && k < nd.nblocks; ++k) load(k);
   for (int r = lane; r < nd.rows; r += 32) xs[r] = a.acc[nd.begin + r];
   __syncwarp();
 
   for (int k = 0; k < nd.nblocks; ++k) {
-    if (k + 1 < nd.nblocks) cp_async_wait<1>();
-    else cp_async_wait<0>();
+    // refill the slot block k-1 used (finished last step), then wait for block
+    // k; the groups committed after block k's may stay in flight
+    if (k + nbuf - 1 < nd.nblocks) load(k + nbuf - 1);
+    const int after = min(nbuf - 1, nd.nblocks - 1 - k);
+    switch (after) {
+      case 0: cp_async_wait<0>(); break;
+      case 1: cp_async_wait<1>(); break;
+      case 2: cp_async_wait<2>(); break;
+      case 3: cp_async_wait<3>(); break;
+      case 4: cp_async_wait<4>(); break;
+      default: cp_async_wait<5>(); break;
+    }
     __syncwarp();
-    const unsigned char *p = (k & 1) ? buf1 : buf0;
+    const unsigned char *p = base + (size_t)(k % nbuf) * a.bufbytes;
     const uint32_t *hdr = reinterpret_cast<const uint32_t *>(p);
     const uint32_t nr = hdr[0], nent = hdr[1], row0 = hdr[2], csz = hdr[3];
     const uint32_t *eoff = reinterpret_cast<const uint32_t *>(p + 16);
@@ -233,6 +440,23 @@ __global__ void __launch_bounds__(128) block_kernel(BlockArgs<VT> a, OutT *out) 
     const size_t o_min = o_val + al16(sizeof(VT) * nent);
     const VT *val = reinterpret_cast<const VT *>(p + o_val);
     const VT *minv = reinterpret_cast<const VT *>(p + o_min);
+#ifdef RCHOL_DEVICE_CHECKS
+    if (nr > (uint32_t)BS || (int64_t)row0 + nr > nd.rows || (csz != 2 && csz != 4) || eoff[BS] != nent ||
+        (int64_t)(o_min + sizeof(VT) * TRI) > a.bufbytes) {
+      if (lane == 0) dbg_report("block header (row0)", row0, nd.rows);
+      return;
+    }
+    bool badc = false;
+    for (uint32_t e = eoff[lane]; e < eoff[lane + 1]; ++e) {
+      const uint32_t cc = csz == 2 ? reinterpret_cast<const uint16_t *>(p + o_col)[e]
+                                   : reinterpret_cast<const uint32_t *>(p + o_col)[e];
+      if (cc >= (uint32_t)nd.rows) {
+        dbg_report("block column", cc, nd.rows);
+        badc = true;
+      }
+    }
+    if (__any_sync(0xffffffffu, badc)) return;
+#endif
     VT t = 0;
     if (lane < (int)nr) {
       VT s0 = 0, s1 = 0;
@@ -255,20 +479,177 @@ __global__ void __launch_bounds__(128) block_kernel(BlockArgs<VT> a, OutT *out) 
       }
       t = xs[row0 + lane] - (s0 + s1);
     }
+    // x_lane = sum_c Minv[lane][c] t_c over the stored triangle
     VT c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+    auto term = [&](int c) -> VT {
+      const VT tc = __shfl_sync(0xffffffffu, t, c);
+      const bool in = UPPER ? (lane <= c) : (lane >= c);
+      const int at = tri_col_off(c, UPPER) + (UPPER ? lane : lane - c);
+      return in ? minv[at] * tc : VT(0);
+    };
 #pragma unroll
     for (int c = 0; c < BS; c += 4) {
-      c0 += minv[(c + 0) * BS + lane] * __shfl_sync(0xffffffffu, t, c + 0);
-      c1 += minv[(c + 1) * BS + lane] * __shfl_sync(0xffffffffu, t, c + 1);
-      c2 += minv[(c + 2) * BS + lane] * __shfl_sync(0xffffffffu, t, c + 2);
-      c3 += minv[(c + 3) * BS + lane] * __shfl_sync(0xffffffffu, t, c + 3);
+      c0 += term(c + 0);
+      c1 += term(c + 1);
+      c2 += term(c + 2);
+      c3 += term(c + 3);
     }
     if (lane < (int)nr) xs[row0 + lane] = (c0 + c1) + (c2 + c3);
     __syncwarp();
-    if (k + 2 < nd.nblocks) load(k + 2, (k & 1) ? buf1 : buf0);
   }
   __syncwarp();
   for (int r = lane; r < nd.rows; r += 32) out[nd.begin + r] = (OutT)xs[r];
+}
+
+// acc_i = rhs_i - sum over row i's entries outside its piece, LANES lanes per
+// row (long external rows at the top of the tree); fixed summation order.
+template <typename VT, typename InT, typename OutT, int LANES>
+__global__ void __launch_bounds__(256) ext_lanes_kernel(const int32_t *__restrict__ rows, int64_t nrows,
+                                                        const int64_t *__restrict__ ext_rp,
+                                                        const int32_t *__restrict__ ext_ci,
+                                                        const VT *__restrict__ ext_v, const InT *__restrict__ in,
+                                                        const OutT *out, VT *__restrict__ acc) {
+  const int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / LANES;
+  const int sub = threadIdx.x % LANES;
+  if (t >= nrows) return;  // whole groups leave together (LANES divides 32)
+  const int64_t i = rows[t];
+  const int64_t q1 = ext_rp[i + 1];
+  VT s0 = 0, s1 = 0;
+  int64_t q = ext_rp[i] + sub;
+  for (; q + LANES < q1; q += 2 * LANES) {
+    s0 += ext_v[q] * (VT)out[ext_ci[q]];
+    s1 += ext_v[q + LANES] * (VT)out[ext_ci[q + LANES]];
+  }
+  if (q < q1) s0 += ext_v[q] * (VT)out[ext_ci[q]];
+  VT s = s0 + s1;
+  const unsigned mask = LANES == 32 ? 0xffffffffu : (((1u << LANES) - 1u) << ((threadIdx.x & 31) / LANES * LANES));
+#pragma unroll
+  for (int o = LANES / 2; o; o >>= 1) s += __shfl_xor_sync(mask, s, o, LANES);
+  if (sub == 0) acc[i] = (VT)in[i] - s;
+}
+
+template <typename VT>
+struct TeamArgs {
+  const NodeDesc *nodes;
+  int node0;            // first piece of the stage; piece = node0 + blockIdx.x
+  int bufbytes;         // per-record buffer (16-aligned)
+  int maxchunk;         // chunk sums per parity buffer
+  const unsigned char *blocks;
+  const int64_t *blk_off;
+  const VT *acc;
+};
+
+constexpr int TEAM_RING = 4;  // records in the ring: the solved block's, the next one's, two in flight
+
+// One thread block per piece: warp 0 solves, the other warps sum far entries
+// one block ahead and stream the records in.  One barrier per block.
+template <typename VT, typename OutT, bool UPPER>
+__global__ void __launch_bounds__(512) team_kernel(TeamArgs<VT> a, OutT *out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ht = tid - 32, TH = (int)blockDim.x - 32;  // helper thread index / count
+  unsigned char *ring = smem;
+  VT *part = reinterpret_cast<VT *>(smem + (size_t)TEAM_RING * a.bufbytes);
+  VT *xs = reinterpret_cast<VT *>(reinterpret_cast<unsigned char *>(part) + al16(2 * (size_t)a.maxchunk * sizeof(VT)));
+  const unsigned char *src = a.blocks;
+  const int64_t *boff = a.blk_off + nd.blk0;
+  const int nb = nd.nblocks;
+  constexpr int VSZ = (int)sizeof(VT);
+
+  auto load = [&](int k) {  // helpers only; one commit group per record (empty past the end)
+    if (k < nb) {
+      unsigned char *dst = ring + (size_t)(k % TEAM_RING) * a.bufbytes;
+      const int64_t o0 = boff[k], len = boff[k + 1] - o0;
+      for (int64_t o = (int64_t)ht * 16; o < len; o += (int64_t)TH * 16) cp_async16(dst + o, src + o0 + o);
+    }
+    cp_async_commit();
+  };
+  for (int r = tid; r < nd.rows; r += blockDim.x) xs[r] = a.acc[nd.begin + r];
+  if (warp > 0) {
+    for (int k = 0; k < TEAM_RING - 1; ++k) load(k);
+    cp_async_wait<TEAM_RING - 3>();  // records 0 and 1 are in
+  }
+  __syncthreads();
+
+  for (int k = 0; k < nb; ++k) {
+    if (warp == 0) {
+      const unsigned char *p = ring + (size_t)(k % TEAM_RING) * a.bufbytes;
+      const uint32_t *hdr = reinterpret_cast<const uint32_t *>(p);
+      const uint32_t nr = hdr[0], row0 = hdr[1], prow0 = hdr[2], nnear = hdr[3], nchunk = hdr[4], nfar = hdr[5],
+                     csz = hdr[6];
+      const TeamLayout L = team_layout(nnear, nchunk, nfar, csz, VSZ);
+      VT t = 0;
+      if (lane < (int)nr) {
+        const uint16_t *noff = reinterpret_cast<const uint16_t *>(p + L.o_noff);
+        const unsigned char *ncol = p + L.o_ncol;
+        const VT *nval = reinterpret_cast<const VT *>(p + L.o_nval);
+        const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + L.o_crow);
+        const VT *pk = part + (size_t)(k & 1) * a.maxchunk;
+        VT s0 = 0, s1 = 0;
+        uint32_t e = noff[lane];
+        const uint32_t e1 = noff[lane + 1];
+        for (; e + 1 < e1; e += 2) {
+          s0 += nval[e] * xs[prow0 + ncol[e]];
+          s1 += nval[e + 1] * xs[prow0 + ncol[e + 1]];
+        }
+        if (e < e1) s0 += nval[e] * xs[prow0 + ncol[e]];
+        for (uint32_t c = crow[lane]; c < crow[lane + 1]; ++c) s1 += pk[c];
+        t = xs[row0 + lane] - (s0 + s1);
+      }
+      const VT *minv = reinterpret_cast<const VT *>(p + L.o_min);
+      VT c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+      auto term = [&](int c) -> VT {
+        const VT tc = __shfl_sync(0xffffffffu, t, c);
+        const bool in = UPPER ? (lane <= c) : (lane >= c);
+        const int at = tri_col_off(c, UPPER) + (UPPER ? lane : lane - c);
+        return in ? minv[at] * tc : VT(0);
+      };
+#pragma unroll
+      for (int c = 0; c < BS; c += 4) {
+        c0 += term(c + 0);
+        c1 += term(c + 1);
+        c2 += term(c + 2);
+        c3 += term(c + 3);
+      }
+      if (lane < (int)nr) xs[row0 + lane] = (c0 + c1) + (c2 + c3);
+    } else {
+      if (k + 1 < nb) {  // far sums of block k+1: columns in blocks solved before block k
+        const unsigned char *p = ring + (size_t)((k + 1) % TEAM_RING) * a.bufbytes;
+        const uint32_t *hdr = reinterpret_cast<const uint32_t *>(p);
+        const uint32_t nnear = hdr[3], nchunk = hdr[4], nfar = hdr[5], csz = hdr[6];
+        const TeamLayout L = team_layout(nnear, nchunk, nfar, csz, VSZ);
+        const uint32_t *cbeg = reinterpret_cast<const uint32_t *>(p + L.o_cbeg);
+        const VT *fval = reinterpret_cast<const VT *>(p + L.o_fval);
+        VT *pk = part + (size_t)((k + 1) & 1) * a.maxchunk;
+        for (int c = ht; c < (int)nchunk; c += TH) {
+          VT s0 = 0, s1 = 0;
+          uint32_t e = cbeg[c];
+          const uint32_t e1 = cbeg[c + 1];
+          if (csz == 2) {
+            const uint16_t *col = reinterpret_cast<const uint16_t *>(p + L.o_fcol);
+            for (; e + 1 < e1; e += 2) {
+              s0 += fval[e] * xs[col[e]];
+              s1 += fval[e + 1] * xs[col[e + 1]];
+            }
+            if (e < e1) s0 += fval[e] * xs[col[e]];
+          } else {
+            const uint32_t *col = reinterpret_cast<const uint32_t *>(p + L.o_fcol);
+            for (; e + 1 < e1; e += 2) {
+              s0 += fval[e] * xs[col[e]];
+              s1 += fval[e + 1] * xs[col[e + 1]];
+            }
+            if (e < e1) s0 += fval[e] * xs[col[e]];
+          }
+          pk[c] = s0 + s1;
+        }
+      }
+      load(k + TEAM_RING - 1);  // into the slot of record k-1, retired last step
+      cp_async_wait<TEAM_RING - 3>();  // records up to k+2 are in
+    }
+    __syncthreads();
+  }
+  for (int r = tid; r < nd.rows; r += blockDim.x) out[nd.begin + r] = (OutT)xs[r];
 }
 
 }  // namespace
@@ -284,24 +665,34 @@ struct HostStreamCopy {
   std::vector<int32_t> ext_ci;
   std::vector<double> ext_v;
   std::vector<int> stage_ptr;
+  std::vector<int> stage_team;
 };
 
 static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
                               const std::vector<double> &v, int64_t n, const std::vector<TreeNode> &tnodes,
-                              bool upper, bool fp32, StreamDir &D, cudaStream_t s,
+                              bool upper, bool fp32, int team_mode, StreamDir &D, cudaStream_t s,
                               HostStreamCopy *host_copy = nullptr) {
   const size_t vsz = fp32 ? 4 : 8;
-  // Pieces: a node is cut into consecutive pieces (whole blocks) so that one
-  // warp's shared memory holds the piece's unknowns plus two block buffers.
-  // The bound of a block record counts every entry of its rows that lies in
-  // the node but outside the block (an upper bound of its sparse part).
+  // Pieces: a node is cut into consecutive pieces (whole blocks) so that the
+  // shared memory of its solver holds the piece's unknowns plus its record
+  // buffers: two for the warp format (more at launch where room is left),
+  // the ring and the chunk sums for the team format.  The bound of a block
+  // record counts every entry of its rows that lies in the node but outside
+  // the block (an upper bound of its sparse part).
   const size_t budget = 200 * 1024;
+  const int helper_threads = 32 * (D.team_warps - 1);
   int maxdepth = 1;
   for (auto &nd : tnodes) maxdepth = std::max(maxdepth, nd.depth);
+  // team format for separators (few, long chains), warp format for leaves
+  auto team_depth = [&](int depth) {
+    if (team_mode == 0) return false;
+    return team_mode == 2 || depth < maxdepth;
+  };
   struct Piece {
     int64_t b, e;
+    bool team;
   };
-  auto cut_node = [&](int64_t b, int64_t e) {
+  auto cut_node = [&](int64_t b, int64_t e, bool team) {
     std::vector<Piece> out;
     const int64_t nb = (e - b + BS - 1) / BS;
     std::vector<size_t> recb(nb);
@@ -311,9 +702,12 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
         size_t cnt = 0;
         for (int64_t i = r0; i < r1; ++i)
           for (int64_t q = rp[i]; q < rp[i + 1]; ++q) cnt += (ci[q] >= b && ci[q] < e && (ci[q] < r0 || ci[q] >= r1));
-        recb[k] = 16 + al16(4 * (BS + 1)) + al16(4 * cnt) + al16(vsz * cnt) + al16(vsz * BS * BS);
+        recb[k] = team ? team_record_bound(cnt, helper_threads, vsz, e - b > 65535 ? 4 : 2)
+                       : 16 + al16(4 * (BS + 1)) + al16(4 * cnt) + al16(vsz * cnt) + al16(vsz * TRI);
       }
     }, 256);
+    const size_t fixed = team ? 2 * al16((size_t)(helper_threads + BS) * vsz) : 0;
+    const size_t nrec = team ? TEAM_RING : 2;
     int64_t k = 0;
     while (k < nb) {
       int64_t k1 = k;
@@ -321,30 +715,46 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
       while (k1 < nb) {
         const size_t m2 = std::max(mx, recb[k1]);
         const int64_t rows = std::min(e, b + (k1 + 1) * BS) - (b + k * BS);
-        if (k1 > k && (2 * al16(m2) + (size_t)rows * vsz > budget || rows > 65535)) break;
+        if (k1 > k && (fixed + nrec * al16(m2) + (size_t)rows * vsz > budget || rows > 65535)) break;
         mx = m2;
         ++k1;
       }
-      if (2 * al16(mx) + (size_t)(std::min(e, b + k1 * BS) - (b + k * BS)) * vsz > budget)
+      if (fixed + nrec * al16(mx) + (size_t)(std::min(e, b + k1 * BS) - (b + k * BS)) * vsz > budget)
         throw Error(RCHOL_ERR_INTERNAL, "a 32-row block of G is too dense for the shared-memory solve");
-      out.push_back(Piece{b + k * BS, std::min(e, b + k1 * BS)});
+      out.push_back(Piece{b + k * BS, std::min(e, b + k1 * BS), team});
       k = k1;
     }
     return out;
   };
   std::vector<Piece> pieces;
+  std::vector<char> team_failed(maxdepth + 1, 0);
   D.stage_ptr.assign(1, 0);
   for (int st = 0; st < maxdepth; ++st) {
     const int depth = upper ? st + 1 : maxdepth - st;
     std::vector<std::vector<Piece>> by_index;  // piece j of every node of this depth
+    bool retry_depth = false;
     for (auto &nd : tnodes) {
       if (nd.depth != depth) continue;
       const int64_t b = nd.begin, e = std::min(nd.end, n);
       if (e <= b) continue;
-      std::vector<Piece> ps = cut_node(b, e);
+      std::vector<Piece> ps;
+      bool team = team_depth(depth) && !team_failed[depth];
+      try {
+        ps = cut_node(b, e, team);
+      } catch (const Error &) {
+        if (!team) throw;
+        // a block too dense for the team ring: this depth uses the warp format
+        team_failed[depth] = true;
+        retry_depth = true;
+        break;
+      }
       if (upper) std::reverse(ps.begin(), ps.end());  // backward: last piece first
       if (by_index.size() < ps.size()) by_index.resize(ps.size());
       for (size_t j = 0; j < ps.size(); ++j) by_index[j].push_back(ps[j]);
+    }
+    if (retry_depth) {
+      --st;  // the same depth again, in the warp format
+      continue;
     }
     for (auto &grp : by_index) {
       for (auto &pc : grp) pieces.push_back(pc);
@@ -383,8 +793,14 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   }, 1 << 14);
   // block records
   std::vector<PieceBuild> built(np);
+  std::vector<int32_t> chunks(np, 0);
   parallel_for(np, [&](int64_t k0, int64_t k1) {
-    for (int64_t k = k0; k < k1; ++k) build_piece(rp, ci, v, pieces[k].b, pieces[k].e, upper, vsz, built[k]);
+    for (int64_t k = k0; k < k1; ++k) {
+      if (pieces[k].team)
+        build_team_piece(rp, ci, v, pieces[k].b, pieces[k].e, upper, vsz, helper_threads, built[k], chunks[k]);
+      else
+        build_piece(rp, ci, v, pieces[k].b, pieces[k].e, upper, vsz, built[k]);
+    }
   }, 1);
   std::vector<NodeDesc> desc(np);
   std::vector<int64_t> blk_off;
@@ -397,6 +813,8 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     desc[k].blk0 = (int64_t)blk_off.size();
     desc[k].maxrec = built[k].maxrec;
     desc[k].wide = desc[k].rows > 65535;
+    desc[k].maxchunk = chunks[k];
+    desc[k].pad_ = 0;
     for (int64_t o : built[k].offs) blk_off.push_back(total + o);
     total += (int64_t)built[k].bytes.size();
     D.sparse_nnz += built[k].sparse;
@@ -408,23 +826,33 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   }, 1);
   built.clear();
   // stages
-  D.stage_split.clear();
   D.stage_rows.clear();
   D.stage_maxrec.clear();
+  D.stage_team.clear();
+  D.stage_chunks.clear();
+  D.stage_ext_lanes.clear();
   D.stage_row_ptr.assign(1, 0);
   D.steps = 0;
   std::vector<int32_t> srows;
   for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
-    int rows = 0, maxrec = 16, steps = 0;
+    int rows = 0, maxrec = 16, steps = 0, maxchunk = 0;
+    int64_t ext = 0, nrow = 0;
     for (int k = D.stage_ptr[st]; k < D.stage_ptr[st + 1]; ++k) {
       rows = std::max(rows, desc[k].rows);
       maxrec = std::max(maxrec, desc[k].maxrec);
       steps = std::max(steps, desc[k].nblocks);
+      maxchunk = std::max(maxchunk, desc[k].maxchunk);
       for (int64_t i = desc[k].begin; i < desc[k].begin + desc[k].rows; ++i) srows.push_back((int32_t)i);
+      ext += ext_rp[desc[k].begin + desc[k].rows] - ext_rp[desc[k].begin];
+      nrow += desc[k].rows;
     }
-    D.stage_split.push_back(1);
+    const bool team = D.stage_ptr[st + 1] > D.stage_ptr[st] && pieces[D.stage_ptr[st]].team;
+    const double avg = nrow ? (double)ext / (double)nrow : 0.0;
     D.stage_rows.push_back(rows);
     D.stage_maxrec.push_back(maxrec);
+    D.stage_team.push_back(team ? 1 : 0);
+    D.stage_chunks.push_back(std::max(1, maxchunk));
+    D.stage_ext_lanes.push_back(avg < 6 ? 1 : avg < 24 ? 4 : avg < 96 ? 8 : 32);
     D.stage_row_ptr.push_back((int64_t)srows.size());
     D.steps += steps;
   }
@@ -438,6 +866,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     host_copy->ext_ci = eci;
     host_copy->ext_v = ev;
     host_copy->stage_ptr = D.stage_ptr;
+    host_copy->stage_team = D.stage_team;
     return;
   }
   D.blocks.upload(all.data(), all.size(), s);
@@ -459,6 +888,9 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
 void build_streams(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
   const int64_t n = F.n, nnz = F.nnz;
   const bool fp32 = F.precision == RCHOL_PREC_FP32;
+#ifdef RCHOL_DEVICE_CHECKS
+  RCHOL_CUDA(cudaMemcpyToSymbol(dbg_n, &n, sizeof(n)));
+#endif
   std::vector<int64_t> rp(n + 1);
   std::vector<int32_t> ci(nnz);
   std::vector<double> v(nnz);
@@ -466,12 +898,20 @@ void build_streams(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
   F.lci.download(ci.data(), nnz, s);
   F.lv.download(v.data(), nnz, s);
   RCHOL_CUDA(cudaStreamSynchronize(s));
-  build_dir_streams(rp, ci, v, n, F.nodes, false, fp32, P.sfwd, s);
+  // Schedule knobs (tuning only; every setting solves exactly the same
+  // system): RCHOL_TRSV_TEAM = 0 warp format everywhere, 1 team format for
+  // separators, 2 team format everywhere (default); RCHOL_TRSV_TEAM_WARPS =
+  // warps of a team (2..16, default 8).
+  int team_mode = 2, team_warps = 8;
+  if (const char *e = getenv("RCHOL_TRSV_TEAM")) team_mode = std::max(0, std::min(2, atoi(e)));
+  if (const char *e = getenv("RCHOL_TRSV_TEAM_WARPS")) team_warps = std::max(2, std::min(16, atoi(e)));
+  P.sfwd.team_warps = P.sbwd.team_warps = team_warps;
+  build_dir_streams(rp, ci, v, n, F.nodes, false, fp32, team_mode, P.sfwd, s);
   F.urp.download(rp.data(), n + 1, s);
   F.uci.download(ci.data(), nnz, s);
   F.uv.download(v.data(), nnz, s);
   RCHOL_CUDA(cudaStreamSynchronize(s));
-  build_dir_streams(rp, ci, v, n, F.nodes, true, fp32, P.sbwd, s);
+  build_dir_streams(rp, ci, v, n, F.nodes, true, fp32, team_mode, P.sbwd, s);
 }
 
 // ---- launch ------------------------------------------------------------------------------
@@ -484,7 +924,14 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
   const int smem_cap = 220 * 1024;
   static bool attr = false;
   if (!attr) {
-    RCHOL_CUDA(cudaFuncSetAttribute(block_kernel<VT, OutT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_cap));
+    RCHOL_CUDA(cudaFuncSetAttribute(block_kernel<VT, OutT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem_cap));
+    RCHOL_CUDA(cudaFuncSetAttribute(block_kernel<VT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem_cap));
+    RCHOL_CUDA(cudaFuncSetAttribute(team_kernel<VT, OutT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem_cap));
+    RCHOL_CUDA(cudaFuncSetAttribute(team_kernel<VT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem_cap));
     attr = true;
   }
   BlockArgs<VT> a;
@@ -492,23 +939,64 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
   a.blocks = D.blocks.p;
   a.blk_off = D.blk_off.p;
   a.acc = acc;
+  a.upper = upper;
+  TeamArgs<VT> ta;
+  ta.nodes = D.nodes.p;
+  ta.blocks = D.blocks.p;
+  ta.blk_off = D.blk_off.p;
+  ta.acc = acc;
   for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
     const int pieces = D.stage_ptr[st + 1] - D.stage_ptr[st];
     if (!pieces) continue;
-    const int64_t r0 = D.stage_row_ptr[st], r1 = D.stage_row_ptr[st + 1];
-    ext_kernel<VT, InT, OutT><<<(unsigned)((r1 - r0 + 255) / 256), 256, 0, s>>>(
-        D.srows.p + r0, r1 - r0, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
+    const int64_t r0 = D.stage_row_ptr[st], r1 = D.stage_row_ptr[st + 1], nr = r1 - r0;
+    const int lanes = D.stage_ext_lanes[st];
+    const unsigned eg = (unsigned)((nr * lanes + 255) / 256);
+    switch (lanes) {
+      case 1:
+        ext_kernel<VT, InT, OutT><<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
+        break;
+      case 4:
+        ext_lanes_kernel<VT, InT, OutT, 4>
+            <<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
+        break;
+      case 8:
+        ext_lanes_kernel<VT, InT, OutT, 8>
+            <<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
+        break;
+      default:
+        ext_lanes_kernel<VT, InT, OutT, 32>
+            <<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
+        break;
+    }
     note_launch();
-    a.node0 = D.stage_ptr[st];
-    a.node1 = D.stage_ptr[st + 1];
-    a.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
-    a.per_warp = (int)al16(2 * (size_t)a.bufbytes + (size_t)D.stage_rows[st] * sizeof(VT));
-    int wpb = std::max(1, std::min(4, smem_cap / a.per_warp));
-    if (a.per_warp > smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
-    wpb = std::min(wpb, pieces);
-    a.wpb = wpb;
-    const int grid = (pieces + wpb - 1) / wpb;
-    block_kernel<VT, OutT><<<grid, 32 * wpb, (size_t)a.per_warp * wpb, s>>>(a, out);
+    const size_t xs_bytes = (size_t)D.stage_rows[st] * sizeof(VT);
+    if (D.stage_team[st]) {
+      ta.node0 = D.stage_ptr[st];
+      ta.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
+      ta.maxchunk = D.stage_chunks[st];
+      const size_t bytes = (size_t)TEAM_RING * ta.bufbytes + al16(2 * (size_t)ta.maxchunk * sizeof(VT)) + xs_bytes;
+      if (bytes > (size_t)smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
+      const unsigned threads = 32u * (unsigned)D.team_warps;
+      if (upper) team_kernel<VT, OutT, true><<<pieces, threads, bytes, s>>>(ta, out);
+      else team_kernel<VT, OutT, false><<<pieces, threads, bytes, s>>>(ta, out);
+    } else {
+      a.node0 = D.stage_ptr[st];
+      a.node1 = D.stage_ptr[st + 1];
+      a.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
+      // deep rings for the few long chains at the top of the tree (latency),
+      // shallower ones where many pieces share an SM (they hide each other)
+      int nbuf = pieces >= 256 ? 4 : 6;
+      while (nbuf > 2 && (size_t)nbuf * a.bufbytes + xs_bytes > (size_t)smem_cap) --nbuf;
+      a.nbuf = nbuf;
+      a.per_warp = (int)al16((size_t)nbuf * a.bufbytes + xs_bytes);
+      int wpb = std::max(1, std::min(4, smem_cap / a.per_warp));
+      if (a.per_warp > smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
+      wpb = std::min(wpb, pieces);
+      a.wpb = wpb;
+      const int grid = (pieces + wpb - 1) / wpb;
+      if (upper) block_kernel<VT, OutT, true><<<grid, 32 * wpb, (size_t)a.per_warp * wpb, s>>>(a, out);
+      else block_kernel<VT, OutT, false><<<grid, 32 * wpb, (size_t)a.per_warp * wpb, s>>>(a, out);
+    }
     note_launch();
     RCHOL_CUDA(cudaGetLastError());
   }

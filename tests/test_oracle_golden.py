@@ -40,6 +40,12 @@ def test_oracle_matches_golden(O, path):
     assert itr == int(g["itr"])
     assert relres == float(g["relres"])
     assert np.array_equal(x, g["x"])
+    # the rounding-order variants used to measure the reproducibility floor
+    # solve the same system: same iteration count, iterate within 1e-9
+    for threads in (8, -8):
+        xv, _, itv = O.pcg(Ap, g["b"], float(g["tol"]), 200, G, threads=threads)
+        assert itv == itr
+        assert np.linalg.norm(xv - x) <= 1e-9 * np.linalg.norm(x)
 
 
 def test_philox_known_answers(O):
