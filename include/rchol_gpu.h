@@ -127,6 +127,17 @@ int rchol_gpu_pcg_d(rchol_matrix_t A, rchol_factor_t G, const double *d_b, doubl
 /* z = (G G^T)^-1 r (c++/util/pcg.cpp:141-159); device pointers. */
 int rchol_gpu_precond_d(rchol_factor_t G, const double *d_r, double *d_z, int64_t nrhs,
                         void *stream);
+/* z = (G G^T)^-1 r for one right-hand side without allocating any memory.
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory at solve time (a memory budget fixed at start-up, allocator-free
+ * real-time loops, hosts that own all device memory): the two scratch vectors
+ * live in a fixed 16 MiB device array inside the library, held on every GPU
+ * that loads it until the process exits, so n is limited to 1,048,576 for an
+ * FP64 factor and 2,097,152 for an FP32 one (larger n: RCHOL_ERR_INVALID).
+ * The first call on a device looks up the array's device address (make it
+ * before any stream capture).  All calls share the array: calls that overlap
+ * on the GPU race.  Device pointers. */
+int rchol_gpu_precond_noalloc_d(rchol_factor_t G, const double *d_r, double *d_z, void *stream);
 /* Forward (y = G^-1 r) or backward (z = G^-T y) solve alone; device pointers. */
 int rchol_gpu_trsv_d(rchol_factor_t G, int transpose, const double *d_in, double *d_out,
                      int64_t nrhs, void *stream);

@@ -51,6 +51,7 @@ SIGNATURES = [
     ("rchol_gpu_pcg", C.c_int, [_vp, _vp, _dp, _dp, _i64, C.c_double, C.c_int, _dp, _ip]),
     ("rchol_gpu_pcg_d", C.c_int, [_vp, _vp, _vp, _vp, _i64, C.c_double, C.c_int, _dp, _ip, _vp]),
     ("rchol_gpu_precond_d", C.c_int, [_vp, _vp, _vp, _i64, _vp]),
+    ("rchol_gpu_precond_noalloc_d", C.c_int, [_vp, _vp, _vp, _vp]),
     ("rchol_gpu_trsv_d", C.c_int, [_vp, C.c_int, _vp, _vp, _i64, _vp]),
     ("rchol_gpu_spmv_d", C.c_int, [_vp, _vp, _vp, _i64, _vp]),
     ("rchol_gpu_edge_grad_d", C.c_int, [_i64, _vp, _vp, _vp, _vp, _vp, _vp]),

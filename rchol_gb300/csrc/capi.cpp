@@ -31,6 +31,7 @@ void pcg_host(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b,
 int64_t plan_levels(const rchol_factor_s &F, bool upper);
 void edge_grad(int64_t m, const int64_t *ei, const int64_t *ej, const double *lam, const double *x, double *g,
                cudaStream_t s);
+void precond_noalloc(const rchol_factor_s &F, const double *r, double *z, cudaStream_t s);
 
 }  // namespace rchol
 
@@ -284,6 +285,13 @@ int rchol_gpu_precond_d(rchol_factor_t G, const double *d_r, double *d_z, int64_
   RCHOL_CHECK_ARG(G && d_r && d_z, "null argument");
   RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   precond(*G, d_r, d_z, (int)nrhs, as_stream(stream));
+  API_END
+}
+
+int rchol_gpu_precond_noalloc_d(rchol_factor_t G, const double *d_r, double *d_z, void *stream) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(G && G->plan && d_r && d_z, "null argument");
+  precond_noalloc(*G, d_r, d_z, as_stream(stream));
   API_END
 }
 

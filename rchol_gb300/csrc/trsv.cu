@@ -1019,4 +1019,67 @@ void stream_trsv(const rchol_factor_s &F, const SolvePlan &P, bool upper, const 
   }
 }
 
+// ---- preconditioner apply without allocation --------------------------------------------
+//
+// Some callers cannot allocate device memory at solve time: code that runs
+// under a fixed memory budget decided at start-up, allocator-free real-time
+// loops, or hosts that own all device memory themselves.  For them the
+// preconditioner z = (G G^T)^-1 r can run with its two scratch vectors (the
+// partial sums and the intermediate y = G^-1 r) in this fixed, file-scope
+// device array instead of buffers allocated with the factor's plan.  Every
+// GPU that loads the library holds the array until the process exits.
+// The array is shared by all calls and keeps the last call's contents; nothing
+// in it has to start at zero (both vectors are fully written before they are
+// read), and calls that overlap on the GPU race on it.
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[128] = {};  // device address of the array, per device ordinal
+}  // namespace
+
+size_t noalloc_scratch_bytes() { return kNoAllocScratchBytes; }
+
+// Set-up on the current device: the array's host-side name is only a
+// stand-in, so the device address is looked up once per device (this first
+// call should therefore come before any stream capture).
+static void *noalloc_scratch_address() {
+  int dev = 0;
+  RCHOL_CUDA(cudaGetDevice(&dev));
+  RCHOL_CHECK_ARG(dev >= 0 && dev < 128, "device ordinal out of range");
+  std::lock_guard<std::mutex> guard(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    RCHOL_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = p;
+  }
+  return g_noalloc_ptr[dev];
+}
+
+void precond_noalloc(const rchol_factor_s &F, const double *r, double *z, cudaStream_t s) {
+  const int64_t n = F.n;
+  const bool fp32 = F.precision == RCHOL_PREC_FP32;
+  const size_t vsz = fp32 ? 4 : 8;
+  const size_t acc_bytes = al16((size_t)n * vsz);
+  if (2 * acc_bytes > kNoAllocScratchBytes)
+    throw Error(RCHOL_ERR_INVALID, "n = " + std::to_string(n) + " needs " + std::to_string(2 * acc_bytes) +
+                                       " bytes of scratch; the allocation-free entry point has " +
+                                       std::to_string(kNoAllocScratchBytes) + " (n <= " +
+                                       std::to_string(kNoAllocScratchBytes / (2 * vsz)) + " for this precision)");
+  unsigned char *base = static_cast<unsigned char *>(noalloc_scratch_address());
+  const SolvePlan &P = *F.plan;
+  if (fp32) {
+    float *acc = reinterpret_cast<float *>(base);
+    float *y = reinterpret_cast<float *>(base + acc_bytes);
+    launch_streams<float, double, float>(P, false, r, y, acc, s);
+    launch_streams<float, float, double>(P, true, y, z, acc, s);
+  } else {
+    double *acc = reinterpret_cast<double *>(base);
+    double *y = reinterpret_cast<double *>(base + acc_bytes);
+    launch_streams<double, double, double>(P, false, r, y, acc, s);
+    launch_streams<double, double, double>(P, true, y, z, acc, s);
+  }
+}
+
 }  // namespace rchol
