@@ -94,6 +94,8 @@ struct SolvePlan {
   std::vector<std::unique_ptr<PcgWork>> pcg;
   DirPlan fwd, bwd;
   StreamDir sfwd, sbwd;
+  StreamDir kfwd, kbwd;    // pieces for up to 32 right-hand sides (built on first use)
+  bool kbuilt = false;
   DevBuf<double> dinv;
   DevBuf<float> dinv32;
   int64_t dag_fwd = 0, dag_bwd = 0;
@@ -103,9 +105,16 @@ struct SolvePlan {
   DevBuf<float> ytmp32;    // intermediate of precond (FP32 path)
   DevBuf<double> acc64;    // external partial sums of split stages
   DevBuf<float> acc32;
+  DevBuf<double> acck64;   // the same for up to 32 right-hand sides (n x 32)
+  DevBuf<float> acck32;
 };
 
 void build_streams(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s);
+void build_streams_k(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s);
+// Solve with G (upper = false) or G^T for k right-hand sides, n x k
+// row-major, in groups of up to 32 columns.
+void stream_trsv_k(const rchol_factor_s &F, const SolvePlan &P, bool upper, const double *in64,
+                   const float *in32, double *out64, float *out32, int k, cudaStream_t s);
 void stream_trsv(const rchol_factor_s &F, const SolvePlan &P, bool upper, const double *in64,
                  const float *in32, double *out64, float *out32, cudaStream_t s);
 

@@ -736,21 +736,20 @@ static void precond_ready(const rchol_factor_s &F, const double *r, double *z, i
 void trsv(const rchol_factor_s &F, bool upper, const double *in, double *out, int k, cudaStream_t s) {
   SolvePlan &P = *F.plan;
   std::lock_guard<std::mutex> guard(P.lock);
-  bool fp32 = F.precision == RCHOL_PREC_FP32;
-  ensure_scratch(P, fp32, F.n * k);
+  ensure_scratch(P, F.precision == RCHOL_PREC_FP32, F.n * k);
   if (k == 1) {
-    if (fp32) stream_trsv(F, P, upper, in, nullptr, out, nullptr, s);
-    else stream_trsv(F, P, upper, in, nullptr, out, nullptr, s);
+    stream_trsv(F, P, upper, in, nullptr, out, nullptr, s);
     return;
   }
-  if (fp32) run_trsv<float, double, double>(F, P, upper, in, out, k, s);
-  else run_trsv<double, double, double>(F, P, upper, in, out, k, s);
+  build_streams_k(F, P, s);
+  stream_trsv_k(F, P, upper, in, nullptr, out, nullptr, k, s);
 }
 
 void precond(const rchol_factor_s &F, const double *r, double *z, int k, cudaStream_t s) {
   SolvePlan &P = *F.plan;
   std::lock_guard<std::mutex> guard(P.lock);
   ensure_scratch(P, F.precision == RCHOL_PREC_FP32, F.n * k);
+  if (k > 1) build_streams_k(F, P, s);
   precond_ready(F, r, z, k, s);
 }
 
@@ -768,11 +767,11 @@ static void precond_ready(const rchol_factor_s &F, const double *r, double *z, i
     return;
   }
   if (fp32) {
-    run_trsv<float, double, float>(F, P, false, r, P.ytmp32.p, k, s);
-    run_trsv<float, float, double>(F, P, true, P.ytmp32.p, z, k, s);
+    stream_trsv_k(F, P, false, r, nullptr, nullptr, P.ytmp32.p, k, s);
+    stream_trsv_k(F, P, true, nullptr, P.ytmp32.p, z, nullptr, k, s);
   } else {
-    run_trsv<double, double, double>(F, P, false, r, P.ytmp.p, k, s);
-    run_trsv<double, double, double>(F, P, true, P.ytmp.p, z, k, s);
+    stream_trsv_k(F, P, false, r, nullptr, P.ytmp.p, nullptr, k, s);
+    stream_trsv_k(F, P, true, P.ytmp.p, nullptr, z, nullptr, k, s);
   }
 }
 
@@ -890,6 +889,7 @@ static void pcg_impl(const rchol_matrix_s &A, const rchol_factor_s &F, const dou
   const int64_t n = A.n, nk = n * k;
   const bool fp32 = F.precision == RCHOL_PREC_FP32;
   ensure_scratch(P, fp32, nk);
+  if (k > 1) build_streams_k(F, P, s);
   if (fp32 ? P.acc32.n < (size_t)n : P.acc64.n < (size_t)n) {
     if (fp32) P.acc32.alloc(n);
     else P.acc64.alloc(n);

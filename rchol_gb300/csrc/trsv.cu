@@ -169,7 +169,9 @@ void build_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
 // being solved ("far" entries), in chunks of near-equal length.  The solver
 // then only adds the previous block's entries ("near") and the chunk sums of
 // its row before applying the inverse.  Record (16-byte aligned sections):
-//   u32 hdr[8]   nrows, row0, prev_row0, nnear, nchunk, nfar, col_bytes, 0
+//   u32 hdr[16]  nrows, row0, prev_row0, nnear, nchunk, nfar, col_bytes, 0,
+//                then the byte offsets of near_col, near_val, chunk_row,
+//                chunk_beg, far_col, far_val, minv and near_off
 //   u16 near_off[33]       lane r's near entries [near_off[r], near_off[r+1])
 //   u8  near_col[nnear]    column inside the previous block (0..31)
 //   VT  near_val[nnear]
@@ -185,7 +187,7 @@ struct TeamLayout {
 __host__ __device__ inline TeamLayout team_layout(uint32_t nnear, uint32_t nchunk, uint32_t nfar, uint32_t csz,
                                                   uint32_t vsz) {
   TeamLayout L;
-  L.o_noff = 32;
+  L.o_noff = 64;
   L.o_ncol = L.o_noff + al16(2 * (BS + 1));
   L.o_nval = L.o_ncol + al16(nnear);
   L.o_crow = L.o_nval + al16((size_t)vsz * nnear);
@@ -202,7 +204,7 @@ __host__ __device__ inline TeamLayout team_layout(uint32_t nnear, uint32_t nchun
 // `helper_threads` threads.
 inline size_t team_record_bound(size_t cnt, size_t helper_threads, size_t vsz, size_t csz) {
   const size_t chunks = std::min(cnt, helper_threads + BS);
-  return 32 + 2 * al16(2 * (BS + 1)) + al16(std::min<size_t>(cnt, BS * BS)) + al16(4 * (chunks + 1)) +
+  return 64 + 2 * al16(2 * (BS + 1)) + al16(std::min<size_t>(cnt, BS * BS)) + al16(4 * (chunks + 1)) +
          al16(csz * cnt) + vsz * cnt + 32 + al16(vsz * TRI);
 }
 
@@ -264,7 +266,10 @@ void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
     const size_t base = P.bytes.size();
     P.bytes.resize(base + L.len, 0);
     unsigned char *p = P.bytes.data() + base;
-    const uint32_t hdr[8] = {(uint32_t)nr, (uint32_t)row0, (uint32_t)prow0, nnear, nchunk, nfar, csz, 0};
+    const uint32_t hdr[16] = {(uint32_t)nr,     (uint32_t)row0,   (uint32_t)prow0,  nnear,
+                              nchunk,           nfar,             csz,              0,
+                              (uint32_t)L.o_ncol, (uint32_t)L.o_nval, (uint32_t)L.o_crow, (uint32_t)L.o_cbeg,
+                              (uint32_t)L.o_fcol, (uint32_t)L.o_fval, (uint32_t)L.o_min,  (uint32_t)L.o_noff};
     std::memcpy(p, hdr, sizeof(hdr));
     auto put_val = [&](size_t off, size_t idx, double x) {
       if (vsz == 8) std::memcpy(p + off + 8 * idx, &x, 8);
@@ -533,16 +538,62 @@ struct TeamArgs {
   const NodeDesc *nodes;
   int node0;            // first piece of the stage; piece = node0 + blockIdx.x
   int bufbytes;         // per-record buffer (16-aligned)
+  int ring;             // records in the ring (4..8): the solved block's, the next one's, ring-2 in flight
   int maxchunk;         // chunk sums per parity buffer
   const unsigned char *blocks;
   const int64_t *blk_off;
   const VT *acc;
 };
 
-constexpr int TEAM_RING = 4;  // records in the ring: the solved block's, the next one's, two in flight
+constexpr int TEAM_RING = 4;  // smallest ring, used to cut pieces; launches deepen it where room is left
+constexpr int TEAM_RING_MAX = 8;
+
+// cp.async.wait_group takes an immediate: wait until at most n groups pend.
+__device__ __forceinline__ void cp_async_wait_upto(int n) {
+  switch (n) {
+    case 0: cp_async_wait<0>(); break;
+    case 1: cp_async_wait<1>(); break;
+    case 2: cp_async_wait<2>(); break;
+    case 3: cp_async_wait<3>(); break;
+    case 4: cp_async_wait<4>(); break;
+    default: cp_async_wait<5>(); break;
+  }
+}
+
+// sum_{e in [e0, e1)} val[e] * x[col[e]] with four independent chains (the
+// column loads of four entries are issued before their gathers).
+template <typename VT, typename CT>
+__device__ __forceinline__ VT chunk_sum(const CT *col, const VT *val, const VT *x, uint32_t e0, uint32_t e1) {
+  VT s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+  uint32_t e = e0;
+  for (; e + 3 < e1; e += 4) {
+    const uint32_t c0 = col[e], c1 = col[e + 1], c2 = col[e + 2], c3 = col[e + 3];
+    s0 += val[e] * x[c0];
+    s1 += val[e + 1] * x[c1];
+    s2 += val[e + 2] * x[c2];
+    s3 += val[e + 3] * x[c3];
+  }
+  for (; e < e1; ++e) s0 += val[e] * x[col[e]];
+  return (s0 + s1) + (s2 + s3);
+}
+
+// Header of a team record, read with four 16-byte loads.
+struct TeamHdr {
+  uint32_t nr, row0, prow0, nnear, nchunk, nfar, csz, pad;
+  uint32_t o_ncol, o_nval, o_crow, o_cbeg, o_fcol, o_fval, o_min, o_noff;
+};
+
+__device__ __forceinline__ TeamHdr read_hdr(const unsigned char *p) {
+  const uint4 *q = reinterpret_cast<const uint4 *>(p);
+  const uint4 a = q[0], b = q[1], c = q[2], d = q[3];
+  return TeamHdr{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
+}
 
 // One thread block per piece: warp 0 solves, the other warps sum far entries
-// one block ahead and stream the records in.  One barrier per block.
+// one block ahead and stream the records in.  One barrier per block.  The
+// solver's step is a latency chain, so everything that does not depend on
+// the previous block (the header, the lane's row of the inverse, its own
+// right-hand side and chunk sums) is loaded before the near entries.
 template <typename VT, typename OutT, bool UPPER>
 __global__ void __launch_bounds__(512) team_kernel(TeamArgs<VT> a, OutT *out) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -550,16 +601,16 @@ __global__ void __launch_bounds__(512) team_kernel(TeamArgs<VT> a, OutT *out) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ht = tid - 32, TH = (int)blockDim.x - 32;  // helper thread index / count
   unsigned char *ring = smem;
-  VT *part = reinterpret_cast<VT *>(smem + (size_t)TEAM_RING * a.bufbytes);
+  const int RING = a.ring;
+  VT *part = reinterpret_cast<VT *>(smem + (size_t)RING * a.bufbytes);
   VT *xs = reinterpret_cast<VT *>(reinterpret_cast<unsigned char *>(part) + al16(2 * (size_t)a.maxchunk * sizeof(VT)));
   const unsigned char *src = a.blocks;
   const int64_t *boff = a.blk_off + nd.blk0;
   const int nb = nd.nblocks;
-  constexpr int VSZ = (int)sizeof(VT);
 
-  auto load = [&](int k) {  // helpers only; one commit group per record (empty past the end)
+  auto load = [&](int k, int slot) {  // helpers only; one commit group per record (empty past the end)
     if (k < nb) {
-      unsigned char *dst = ring + (size_t)(k % TEAM_RING) * a.bufbytes;
+      unsigned char *dst = ring + (size_t)slot * a.bufbytes;
       const int64_t o0 = boff[k], len = boff[k + 1] - o0;
       for (int64_t o = (int64_t)ht * 16; o < len; o += (int64_t)TH * 16) cp_async16(dst + o, src + o0 + o);
     }
@@ -567,89 +618,230 @@ __global__ void __launch_bounds__(512) team_kernel(TeamArgs<VT> a, OutT *out) {
   };
   for (int r = tid; r < nd.rows; r += blockDim.x) xs[r] = a.acc[nd.begin + r];
   if (warp > 0) {
-    for (int k = 0; k < TEAM_RING - 1; ++k) load(k);
-    cp_async_wait<TEAM_RING - 3>();  // records 0 and 1 are in
+    for (int k = 0; k < RING - 1; ++k) load(k, k);
+    cp_async_wait_upto(RING - 3);  // records 0 and 1 are in
   }
   __syncthreads();
 
+  int slot = 0;  // ring slot of record k
   for (int k = 0; k < nb; ++k) {
+    const int next = slot + 1 == RING ? 0 : slot + 1;
     if (warp == 0) {
-      const unsigned char *p = ring + (size_t)(k % TEAM_RING) * a.bufbytes;
-      const uint32_t *hdr = reinterpret_cast<const uint32_t *>(p);
-      const uint32_t nr = hdr[0], row0 = hdr[1], prow0 = hdr[2], nnear = hdr[3], nchunk = hdr[4], nfar = hdr[5],
-                     csz = hdr[6];
-      const TeamLayout L = team_layout(nnear, nchunk, nfar, csz, VSZ);
+      const unsigned char *p = ring + (size_t)slot * a.bufbytes;
+      const TeamHdr h = read_hdr(p);
+      const VT *minv = reinterpret_cast<const VT *>(p + h.o_min);
+      // the lane's row of the inverse (zero outside the triangle)
+      VT m[BS];
+#pragma unroll
+      for (int c = 0; c < BS; ++c) {
+        const bool in = UPPER ? (lane <= c) : (lane >= c);
+        m[c] = minv[in ? tri_col_off(c, UPPER) + (UPPER ? lane : lane - c) : 0];
+        m[c] = in ? m[c] : VT(0);
+      }
       VT t = 0;
-      if (lane < (int)nr) {
-        const uint16_t *noff = reinterpret_cast<const uint16_t *>(p + L.o_noff);
-        const unsigned char *ncol = p + L.o_ncol;
-        const VT *nval = reinterpret_cast<const VT *>(p + L.o_nval);
-        const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + L.o_crow);
+      if (lane < (int)h.nr) {
+        const uint16_t *noff = reinterpret_cast<const uint16_t *>(p + h.o_noff);
+        const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h.o_crow);
         const VT *pk = part + (size_t)(k & 1) * a.maxchunk;
-        VT s0 = 0, s1 = 0;
+        const VT own = xs[h.row0 + lane];
+        VT s1 = 0, s3 = 0;
+        uint32_t c = crow[lane];
+        const uint32_t c1 = crow[lane + 1];
+        for (; c + 1 < c1; c += 2) {
+          s1 += pk[c];
+          s3 += pk[c + 1];
+        }
+        if (c < c1) s1 += pk[c];
+        s1 += s3;
+        const unsigned char *ncol = p + h.o_ncol;
+        const VT *nval = reinterpret_cast<const VT *>(p + h.o_nval);
+        const VT *xp = xs + h.prow0;
+        VT s0 = 0, s2 = 0;
         uint32_t e = noff[lane];
         const uint32_t e1 = noff[lane + 1];
-        for (; e + 1 < e1; e += 2) {
-          s0 += nval[e] * xs[prow0 + ncol[e]];
-          s1 += nval[e + 1] * xs[prow0 + ncol[e + 1]];
+        for (; e + 3 < e1; e += 4) {
+          const unsigned c0 = ncol[e], c1 = ncol[e + 1], c2 = ncol[e + 2], c3 = ncol[e + 3];
+          s0 += nval[e] * xp[c0];
+          s2 += nval[e + 1] * xp[c1];
+          s0 += nval[e + 2] * xp[c2];
+          s2 += nval[e + 3] * xp[c3];
         }
-        if (e < e1) s0 += nval[e] * xs[prow0 + ncol[e]];
-        for (uint32_t c = crow[lane]; c < crow[lane + 1]; ++c) s1 += pk[c];
-        t = xs[row0 + lane] - (s0 + s1);
+        for (; e < e1; ++e) s0 += nval[e] * xp[ncol[e]];
+        t = own - ((s0 + s2) + s1);
       }
-      const VT *minv = reinterpret_cast<const VT *>(p + L.o_min);
       VT c0 = 0, c1 = 0, c2 = 0, c3 = 0;
-      auto term = [&](int c) -> VT {
-        const VT tc = __shfl_sync(0xffffffffu, t, c);
-        const bool in = UPPER ? (lane <= c) : (lane >= c);
-        const int at = tri_col_off(c, UPPER) + (UPPER ? lane : lane - c);
-        return in ? minv[at] * tc : VT(0);
-      };
 #pragma unroll
       for (int c = 0; c < BS; c += 4) {
-        c0 += term(c + 0);
-        c1 += term(c + 1);
-        c2 += term(c + 2);
-        c3 += term(c + 3);
+        c0 += m[c + 0] * __shfl_sync(0xffffffffu, t, c + 0);
+        c1 += m[c + 1] * __shfl_sync(0xffffffffu, t, c + 1);
+        c2 += m[c + 2] * __shfl_sync(0xffffffffu, t, c + 2);
+        c3 += m[c + 3] * __shfl_sync(0xffffffffu, t, c + 3);
       }
-      if (lane < (int)nr) xs[row0 + lane] = (c0 + c1) + (c2 + c3);
+      if (lane < (int)h.nr) xs[h.row0 + lane] = (c0 + c1) + (c2 + c3);
     } else {
       if (k + 1 < nb) {  // far sums of block k+1: columns in blocks solved before block k
-        const unsigned char *p = ring + (size_t)((k + 1) % TEAM_RING) * a.bufbytes;
-        const uint32_t *hdr = reinterpret_cast<const uint32_t *>(p);
-        const uint32_t nnear = hdr[3], nchunk = hdr[4], nfar = hdr[5], csz = hdr[6];
-        const TeamLayout L = team_layout(nnear, nchunk, nfar, csz, VSZ);
-        const uint32_t *cbeg = reinterpret_cast<const uint32_t *>(p + L.o_cbeg);
-        const VT *fval = reinterpret_cast<const VT *>(p + L.o_fval);
+        const unsigned char *p = ring + (size_t)next * a.bufbytes;
+        const TeamHdr h = read_hdr(p);
+        const uint32_t *cbeg = reinterpret_cast<const uint32_t *>(p + h.o_cbeg);
+        const VT *fval = reinterpret_cast<const VT *>(p + h.o_fval);
         VT *pk = part + (size_t)((k + 1) & 1) * a.maxchunk;
-        for (int c = ht; c < (int)nchunk; c += TH) {
-          VT s0 = 0, s1 = 0;
-          uint32_t e = cbeg[c];
-          const uint32_t e1 = cbeg[c + 1];
-          if (csz == 2) {
-            const uint16_t *col = reinterpret_cast<const uint16_t *>(p + L.o_fcol);
-            for (; e + 1 < e1; e += 2) {
-              s0 += fval[e] * xs[col[e]];
-              s1 += fval[e + 1] * xs[col[e + 1]];
-            }
-            if (e < e1) s0 += fval[e] * xs[col[e]];
-          } else {
-            const uint32_t *col = reinterpret_cast<const uint32_t *>(p + L.o_fcol);
-            for (; e + 1 < e1; e += 2) {
-              s0 += fval[e] * xs[col[e]];
-              s1 += fval[e + 1] * xs[col[e + 1]];
-            }
-            if (e < e1) s0 += fval[e] * xs[col[e]];
-          }
-          pk[c] = s0 + s1;
+        for (int c = ht; c < (int)h.nchunk; c += TH) {
+          const uint32_t e0 = cbeg[c], e1 = cbeg[c + 1];
+          pk[c] = h.csz == 2 ? chunk_sum(reinterpret_cast<const uint16_t *>(p + h.o_fcol), fval, xs, e0, e1)
+                             : chunk_sum(reinterpret_cast<const uint32_t *>(p + h.o_fcol), fval, xs, e0, e1);
         }
       }
-      load(k + TEAM_RING - 1);  // into the slot of record k-1, retired last step
-      cp_async_wait<TEAM_RING - 3>();  // records up to k+2 are in
+      // record k+RING-1 goes into the slot of record k-1, retired last step
+      load(k + RING - 1, slot == 0 ? RING - 1 : slot - 1);
+      cp_async_wait_upto(RING - 3);  // records up to k+2 are in
     }
+    slot = next;
     __syncthreads();
   }
   for (int r = tid; r < nd.rows; r += blockDim.x) out[nd.begin + r] = (OutT)xs[r];
+}
+
+// ---- several right-hand sides -----------------------------------------------------
+//
+// Vectors are n x ld row-major; one pass solves k <= KW consecutive columns
+// (acc is n x KW).  Lane j of a warp owns right-hand
+// side j, so every entry of G is read once for all k and applied with one
+// FMA per lane; the piece's unknowns sit in shared memory as rows of KW
+// values.  The records are the team format's, in pieces cut for KW-wide rows.
+
+constexpr int KW = 32;
+
+template <typename VT, typename InT, typename OutT>
+__global__ void __launch_bounds__(256) ext_k_kernel(const int32_t *__restrict__ rows, int64_t nrows,
+                                                   const int64_t *__restrict__ ext_rp,
+                                                   const int32_t *__restrict__ ext_ci, const VT *__restrict__ ext_v,
+                                                   const InT *__restrict__ in, const OutT *out,
+                                                   VT *__restrict__ acc, int k, int64_t ld) {
+  const int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= nrows || lane >= k) return;
+  const int64_t i = rows[t];
+  const int64_t q1 = ext_rp[i + 1];
+  VT s0 = 0, s1 = 0;
+  int64_t q = ext_rp[i];
+  for (; q + 1 < q1; q += 2) {
+    s0 += ext_v[q] * (VT)out[(int64_t)ext_ci[q] * ld + lane];
+    s1 += ext_v[q + 1] * (VT)out[(int64_t)ext_ci[q + 1] * ld + lane];
+  }
+  if (q < q1) s0 += ext_v[q] * (VT)out[(int64_t)ext_ci[q] * ld + lane];
+  acc[i * KW + lane] = (VT)in[i * ld + lane] - (s0 + s1);
+}
+
+// One thread block per piece.  Warp 0 solves block b for all right-hand sides
+// (t = acc - near - far sums, x = T^-1 t with the packed inverse, in
+// registers); helper warps sum the far entries of block b+1 row by row into
+// part[(b+1)&1][row][lane] and stream the records.  One barrier per block.
+template <typename VT, typename OutT, bool UPPER>
+__global__ void __launch_bounds__(256) team_k_kernel(TeamArgs<VT> a, OutT *out, int k, int64_t ld) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ht = tid - 32, TH = (int)blockDim.x - 32, HW = (int)(blockDim.x >> 5) - 1;
+  const int RING = a.ring;
+  unsigned char *ring = smem;
+  VT *part = reinterpret_cast<VT *>(smem + (size_t)RING * a.bufbytes);  // [2][BS][KW]
+  VT *xs = part + 2 * BS * KW;                                           // [rows][KW]
+  const unsigned char *src = a.blocks;
+  const int64_t *boff = a.blk_off + nd.blk0;
+  const int nb = nd.nblocks;
+
+  auto load = [&](int b) {
+    if (b < nb) {
+      unsigned char *dst = ring + (size_t)(b % RING) * a.bufbytes;
+      const int64_t o0 = boff[b], len = boff[b + 1] - o0;
+      for (int64_t o = (int64_t)ht * 16; o < len; o += (int64_t)TH * 16) cp_async16(dst + o, src + o0 + o);
+    }
+    cp_async_commit();
+  };
+  for (int idx = tid; idx < nd.rows * KW; idx += blockDim.x) {
+    const int r = idx / KW, j = idx % KW;
+    xs[idx] = j < k ? a.acc[(nd.begin + r) * (int64_t)KW + j] : VT(0);
+  }
+  for (int idx = tid; idx < 2 * BS * KW; idx += blockDim.x) part[idx] = VT(0);  // block 0 has no far sums
+  if (warp > 0) {
+    for (int b = 0; b < RING - 1; ++b) load(b);
+    cp_async_wait_upto(RING - 3);
+  }
+  __syncthreads();
+
+  for (int b = 0; b < nb; ++b) {
+    if (warp == 0) {
+      const unsigned char *p = ring + (size_t)(b % RING) * a.bufbytes;
+      const TeamHdr h = read_hdr(p);
+      const uint32_t nr = h.nr, row0 = h.row0, prow0 = h.prow0;
+      const uint16_t *noff = reinterpret_cast<const uint16_t *>(p + h.o_noff);
+      const unsigned char *ncol = p + h.o_ncol;
+      const VT *nval = reinterpret_cast<const VT *>(p + h.o_nval);
+      const VT *minv = reinterpret_cast<const VT *>(p + h.o_min);
+      const VT *pb = part + (size_t)(b & 1) * BS * KW;
+      VT t[BS];
+#pragma unroll
+      for (int r = 0; r < BS; ++r) {
+        VT s = 0;
+        if (r < (int)nr) {
+          s = xs[(row0 + r) * KW + lane] - pb[r * KW + lane];
+          for (uint32_t e = noff[r]; e < noff[r + 1]; ++e) s -= nval[e] * xs[(prow0 + ncol[e]) * KW + lane];
+        }
+        t[r] = s;
+      }
+      // x = T^-1 t in place: lower rows from the last up, upper from the first down
+#pragma unroll
+      for (int i = 0; i < BS; ++i) {
+        const int r = UPPER ? i : BS - 1 - i;
+        VT s = 0;
+#pragma unroll
+        for (int c = UPPER ? r : 0; c <= (UPPER ? BS - 1 : r); ++c)
+          s += minv[tri_col_off(c, UPPER) + (UPPER ? r : r - c)] * t[c];
+        t[r] = s;
+      }
+#pragma unroll
+      for (int r = 0; r < BS; ++r)
+        if (r < (int)nr) xs[(row0 + r) * KW + lane] = t[r];
+    } else {
+      if (b + 1 < nb) {
+        const unsigned char *p = ring + (size_t)((b + 1) % RING) * a.bufbytes;
+        const TeamHdr h = read_hdr(p);
+        const uint32_t csz = h.csz;
+        const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h.o_crow);
+        const uint32_t *cbeg = reinterpret_cast<const uint32_t *>(p + h.o_cbeg);
+        const VT *fval = reinterpret_cast<const VT *>(p + h.o_fval);
+        VT *pb = part + (size_t)((b + 1) & 1) * BS * KW;
+        for (int r = warp - 1; r < BS; r += HW) {
+          VT s0 = 0, s1 = 0;
+          uint32_t e = cbeg[crow[r]];
+          const uint32_t e1 = cbeg[crow[r + 1]];
+          if (csz == 2) {
+            const uint16_t *col = reinterpret_cast<const uint16_t *>(p + h.o_fcol);
+            for (; e + 1 < e1; e += 2) {
+              s0 += fval[e] * xs[col[e] * KW + lane];
+              s1 += fval[e + 1] * xs[col[e + 1] * KW + lane];
+            }
+            if (e < e1) s0 += fval[e] * xs[col[e] * KW + lane];
+          } else {
+            const uint32_t *col = reinterpret_cast<const uint32_t *>(p + h.o_fcol);
+            for (; e + 1 < e1; e += 2) {
+              s0 += fval[e] * xs[(size_t)col[e] * KW + lane];
+              s1 += fval[e + 1] * xs[(size_t)col[e + 1] * KW + lane];
+            }
+            if (e < e1) s0 += fval[e] * xs[(size_t)col[e] * KW + lane];
+          }
+          pb[r * KW + lane] = s0 + s1;
+        }
+      }
+      load(b + RING - 1);
+      cp_async_wait_upto(RING - 3);
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < nd.rows * KW; idx += blockDim.x) {
+    const int r = idx / KW, j = idx % KW;
+    if (j < k) out[(nd.begin + r) * ld + j] = (OutT)xs[idx];
+  }
 }
 
 }  // namespace
@@ -670,9 +862,11 @@ struct HostStreamCopy {
 
 static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
                               const std::vector<double> &v, int64_t n, const std::vector<TreeNode> &tnodes,
-                              bool upper, bool fp32, int team_mode, StreamDir &D, cudaStream_t s,
+                              bool upper, bool fp32, int team_mode, int kwidth, StreamDir &D, cudaStream_t s,
                               HostStreamCopy *host_copy = nullptr) {
   const size_t vsz = fp32 ? 4 : 8;
+  const size_t row_bytes = vsz * (size_t)kwidth;  // a piece's unknowns per row in shared memory
+  if (kwidth > 1) team_mode = 2;                  // several right-hand sides: team format only
   // Pieces: a node is cut into consecutive pieces (whole blocks) so that the
   // shared memory of its solver holds the piece's unknowns plus its record
   // buffers: two for the warp format (more at launch where room is left),
@@ -706,7 +900,9 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
                        : 16 + al16(4 * (BS + 1)) + al16(4 * cnt) + al16(vsz * cnt) + al16(vsz * TRI);
       }
     }, 256);
-    const size_t fixed = team ? 2 * al16((size_t)(helper_threads + BS) * vsz) : 0;
+    const size_t fixed = !team ? 0
+                         : kwidth > 1 ? 2 * (size_t)BS * KW * vsz
+                                      : 2 * al16((size_t)(helper_threads + BS) * vsz);
     const size_t nrec = team ? TEAM_RING : 2;
     int64_t k = 0;
     while (k < nb) {
@@ -715,11 +911,11 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
       while (k1 < nb) {
         const size_t m2 = std::max(mx, recb[k1]);
         const int64_t rows = std::min(e, b + (k1 + 1) * BS) - (b + k * BS);
-        if (k1 > k && (fixed + nrec * al16(m2) + (size_t)rows * vsz > budget || rows > 65535)) break;
+        if (k1 > k && (fixed + nrec * al16(m2) + (size_t)rows * row_bytes > budget || rows > 65535)) break;
         mx = m2;
         ++k1;
       }
-      if (fixed + nrec * al16(mx) + (size_t)(std::min(e, b + k1 * BS) - (b + k * BS)) * vsz > budget)
+      if (fixed + nrec * al16(mx) + (size_t)(std::min(e, b + k1 * BS) - (b + k * BS)) * row_bytes > budget)
         throw Error(RCHOL_ERR_INTERNAL, "a 32-row block of G is too dense for the shared-memory solve");
       out.push_back(Piece{b + k * BS, std::min(e, b + k1 * BS), team});
       k = k1;
@@ -742,7 +938,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
       try {
         ps = cut_node(b, e, team);
       } catch (const Error &) {
-        if (!team) throw;
+        if (!team || kwidth > 1) throw;
         // a block too dense for the team ring: this depth uses the warp format
         team_failed[depth] = true;
         retry_depth = true;
@@ -885,7 +1081,9 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   RCHOL_CUDA(cudaStreamSynchronize(s));
 }
 
-void build_streams(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
+// Builds both directions' streams for pieces holding `kwidth` values per row.
+static void build_streams_width(const rchol_factor_s &F, int kwidth, StreamDir &fwd, StreamDir &bwd,
+                                cudaStream_t s) {
   const int64_t n = F.n, nnz = F.nnz;
   const bool fp32 = F.precision == RCHOL_PREC_FP32;
 #ifdef RCHOL_DEVICE_CHECKS
@@ -905,16 +1103,41 @@ void build_streams(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
   int team_mode = 2, team_warps = 8;
   if (const char *e = getenv("RCHOL_TRSV_TEAM")) team_mode = std::max(0, std::min(2, atoi(e)));
   if (const char *e = getenv("RCHOL_TRSV_TEAM_WARPS")) team_warps = std::max(2, std::min(16, atoi(e)));
-  P.sfwd.team_warps = P.sbwd.team_warps = team_warps;
-  build_dir_streams(rp, ci, v, n, F.nodes, false, fp32, team_mode, P.sfwd, s);
+  if (kwidth > 1) team_warps = 8;
+  fwd.team_warps = bwd.team_warps = team_warps;
+  build_dir_streams(rp, ci, v, n, F.nodes, false, fp32, team_mode, kwidth, fwd, s);
   F.urp.download(rp.data(), n + 1, s);
   F.uci.download(ci.data(), nnz, s);
   F.uv.download(v.data(), nnz, s);
   RCHOL_CUDA(cudaStreamSynchronize(s));
-  build_dir_streams(rp, ci, v, n, F.nodes, true, fp32, team_mode, P.sbwd, s);
+  build_dir_streams(rp, ci, v, n, F.nodes, true, fp32, team_mode, kwidth, bwd, s);
+}
+
+void build_streams(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
+  build_streams_width(F, 1, P.sfwd, P.sbwd, s);
+}
+
+// The multi-right-hand-side streams, built on first use.
+void build_streams_k(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
+  if (P.kbuilt) return;
+  build_streams_width(F, KW, P.kfwd, P.kbwd, s);
+  if (F.precision == RCHOL_PREC_FP32) P.acck32.alloc((size_t)F.n * KW);
+  else P.acck64.alloc((size_t)F.n * KW);
+  P.kbuilt = true;
 }
 
 // ---- launch ------------------------------------------------------------------------------
+
+static int sm_count() {
+  static int count = 0;
+  if (!count) {
+    int dev = 0, c = 0;
+    RCHOL_CUDA(cudaGetDevice(&dev));
+    RCHOL_CUDA(cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev));
+    count = std::max(1, c);
+  }
+  return count;
+}
 
 template <typename VT, typename InT, typename OutT>
 static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *out, VT *acc, cudaStream_t s) {
@@ -974,7 +1197,14 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       ta.node0 = D.stage_ptr[st];
       ta.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
       ta.maxchunk = D.stage_chunks[st];
-      const size_t bytes = (size_t)TEAM_RING * ta.bufbytes + al16(2 * (size_t)ta.maxchunk * sizeof(VT)) + xs_bytes;
+      const size_t fixed = al16(2 * (size_t)ta.maxchunk * sizeof(VT)) + xs_bytes;
+      // the deepest ring that fits (records arrive ring-3 steps ahead of use)
+      // where few pieces share the GPU; where many do, they hide each
+      // other's latency and shared memory goes to residency instead
+      int ring = pieces > 2 * sm_count() ? 5 : TEAM_RING_MAX;
+      while (ring > TEAM_RING && fixed + (size_t)ring * ta.bufbytes > (size_t)smem_cap) --ring;
+      ta.ring = ring;
+      const size_t bytes = (size_t)ring * ta.bufbytes + fixed;
       if (bytes > (size_t)smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
       const unsigned threads = 32u * (unsigned)D.team_warps;
       if (upper) team_kernel<VT, OutT, true><<<pieces, threads, bytes, s>>>(ta, out);
@@ -1016,6 +1246,68 @@ void stream_trsv(const rchol_factor_s &F, const SolvePlan &P, bool upper, const 
     if (Pm.acc64.n < (size_t)n) Pm.acc64.alloc(n);
     if (in64 && out64) launch_streams<double, double, double>(P, upper, in64, out64, Pm.acc64.p, s);
     else throw Error(RCHOL_ERR_INTERNAL, "unsupported triangular-solve operand types");
+  }
+}
+
+template <typename VT, typename InT, typename OutT>
+static void launch_streams_k(const SolvePlan &P, bool upper, const InT *in, OutT *out, VT *acc, int k,
+                             int64_t ld, cudaStream_t s) {
+  const StreamDir &D = upper ? P.kbwd : P.kfwd;
+  constexpr bool f64 = sizeof(VT) == 8;
+  const VT *ext_v = reinterpret_cast<const VT *>(f64 ? (const void *)D.ext_v64.p : (const void *)D.ext_v32.p);
+  const int smem_cap = 220 * 1024;
+  static bool attr = false;
+  if (!attr) {
+    RCHOL_CUDA(cudaFuncSetAttribute(team_k_kernel<VT, OutT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem_cap));
+    RCHOL_CUDA(cudaFuncSetAttribute(team_k_kernel<VT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem_cap));
+    attr = true;
+  }
+  TeamArgs<VT> ta;
+  ta.nodes = D.nodes.p;
+  ta.blocks = D.blocks.p;
+  ta.blk_off = D.blk_off.p;
+  ta.acc = acc;
+  ta.maxchunk = 0;
+  for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
+    const int pieces = D.stage_ptr[st + 1] - D.stage_ptr[st];
+    if (!pieces) continue;
+    const int64_t r0 = D.stage_row_ptr[st], r1 = D.stage_row_ptr[st + 1], nr = r1 - r0;
+    ext_k_kernel<VT, InT, OutT><<<(unsigned)((nr * 32 + 255) / 256), 256, 0, s>>>(
+        D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc, k, ld);
+    note_launch();
+    ta.node0 = D.stage_ptr[st];
+    ta.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
+    const size_t fixed = 2 * (size_t)BS * KW * sizeof(VT) + (size_t)D.stage_rows[st] * KW * sizeof(VT);
+    int ring = pieces > 2 * sm_count() ? 5 : TEAM_RING_MAX;
+    while (ring > TEAM_RING && fixed + (size_t)ring * ta.bufbytes > (size_t)smem_cap) --ring;
+    ta.ring = ring;
+    const size_t bytes = (size_t)ring * ta.bufbytes + fixed;
+    if (bytes > (size_t)smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
+    if (upper) team_k_kernel<VT, OutT, true><<<pieces, 256, bytes, s>>>(ta, out, k, ld);
+    else team_k_kernel<VT, OutT, false><<<pieces, 256, bytes, s>>>(ta, out, k, ld);
+    note_launch();
+    RCHOL_CUDA(cudaGetLastError());
+  }
+}
+
+void stream_trsv_k(const rchol_factor_s &F, const SolvePlan &P, bool upper, const double *in64,
+                   const float *in32, double *out64, float *out32, int k, cudaStream_t s) {
+  if (!P.kbuilt) throw Error(RCHOL_ERR_INTERNAL, "multi-right-hand-side streams not built");
+  for (int j0 = 0; j0 < k; j0 += KW) {  // groups of up to KW columns
+    const int kg = std::min(KW, k - j0);
+    if (F.precision == RCHOL_PREC_FP32) {
+      float *acc = P.acck32.p;
+      if (in64 && out32) launch_streams_k<float, double, float>(P, upper, in64 + j0, out32 + j0, acc, kg, k, s);
+      else if (in32 && out64) launch_streams_k<float, float, double>(P, upper, in32 + j0, out64 + j0, acc, kg, k, s);
+      else if (in64 && out64) launch_streams_k<float, double, double>(P, upper, in64 + j0, out64 + j0, acc, kg, k, s);
+      else throw Error(RCHOL_ERR_INTERNAL, "unsupported triangular-solve operand types");
+    } else {
+      if (in64 && out64)
+        launch_streams_k<double, double, double>(P, upper, in64 + j0, out64 + j0, P.acck64.p, kg, k, s);
+      else throw Error(RCHOL_ERR_INTERNAL, "unsupported triangular-solve operand types");
+    }
   }
 }
 

@@ -115,6 +115,47 @@ def test_trsv_forward_backward(case, O):
     assert np.linalg.norm(zp - zo) / np.linalg.norm(zo) < TOL
 
 
+@pytest.mark.parametrize("k", [2, 32, 40])
+def test_trsv_many_rhs(case, O, k):
+    """k right-hand sides (n x k row-major; more than 32 run in groups of 32)
+    against the oracle's single-vector solves, column by column, both
+    directions and the preconditioner, FP64 and FP32 factors."""
+    import torch
+
+    n = case["n"]
+    Rm = np.random.default_rng(7 + k).standard_normal((n, k))
+    L = _lib.lib()
+    dr = _dev(torch, Rm)
+    dy = torch.empty_like(dr)
+    dz = torch.empty_like(dr)
+    st = _stream(torch)
+    _lib.check(L.rchol_gpu_trsv_d(case["F"].ptr, 0, dr.data_ptr(), dy.data_ptr(), k, st))
+    _lib.check(L.rchol_gpu_trsv_d(case["F"].ptr, 1, dr.data_ptr(), dz.data_ptr(), k, st))
+    Y, Z = dy.cpu().numpy(), dz.cpu().numpy()
+    for j in range(k):
+        y_o = O.trsv_lower(case["G"], Rm[:, j].copy())
+        z_o = O.trsv_upper(case["G"], Rm[:, j].copy())
+        assert np.linalg.norm(Y[:, j] - y_o) / np.linalg.norm(y_o) < TOL, j
+        assert np.linalg.norm(Z[:, j] - z_o) / np.linalg.norm(z_o) < TOL, j
+    _lib.check(L.rchol_gpu_precond_d(case["F"].ptr, dr.data_ptr(), dz.data_ptr(), k, st))
+    Z = dz.cpu().numpy()
+    for j in range(k):
+        zo = O.precond(case["G"], Rm[:, j].copy())
+        assert np.linalg.norm(Z[:, j] - zo) / np.linalg.norm(zo) < TOL, j
+    # FP32 factor: the k-vector solve equals the single-vector FP32 solve to FP32 rounding
+    G = case["G"]
+    R = __import__("rchol_gb300")
+    F32 = R.Factor.from_host(G[0], G[1], G[2], case["tree"], precision=R.PREC_FP32)
+    _lib.check(L.rchol_gpu_precond_d(F32.ptr, dr.data_ptr(), dz.data_ptr(), k, st))
+    Z32 = dz.cpu().numpy()
+    z1 = torch.empty(n, dtype=torch.float64, device="cuda")
+    for j in (0, k - 1):
+        r1 = _dev(torch, Rm[:, j].copy())
+        _lib.check(L.rchol_gpu_precond_d(F32.ptr, r1.data_ptr(), z1.data_ptr(), 1, st))
+        zs = z1.cpu().numpy()
+        assert np.linalg.norm(Z32[:, j] - zs) / np.linalg.norm(zs) < 1e-5, j
+
+
 def test_spmv(case, O):
     import torch
 
