@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--cpu-sample-iters", type=int, default=2)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the k-right-hand-side (128^3, k=32) and batched-systems (512 2D grids) lines")
     return p.parse_args()
 
 
@@ -271,6 +273,10 @@ def run_gb300(args, rank, local, world, pg):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, Ap, bp, F64, it64)
+    extras = None
+    if not args.no_extras:
+        del F64, F32, Ad
+        extras = {"k_rhs": run_k_rhs(args, dev), "batched": run_batched(args, dev)}
     if rank != 0:
         return None
     traffic = profile_traffic()
@@ -319,8 +325,107 @@ def run_gb300(args, rank, local, world, pg):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "configs": extras,
     }
     return line
+
+
+def _event_ms(torch, fn, reps, stream):
+    fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_k_rhs(args, dev):
+    """128^3 constant 7-point Laplacian, 32 right-hand sides N(0,1) in one PCG
+    (n x 32 row-major) against 32 single-vector solves; FP32 G."""
+    import torch
+
+    import rchol_gb300 as R
+    from rchol_gb300 import _lib, generators
+
+    L = _lib.lib()
+    A = generators.laplace_3d(128)
+    n, k = A.shape[0], 32
+    tree = R.Tree.build(A.indptr, A.indices, 256)
+    Ad = R.Matrix.create(A.indptr, A.indices, A.data, tree)
+    F = R.Factor.compute(Ad, tree, seed=args.seed, precision=R.PREC_FP32)
+    B = torch.tensor(np.random.default_rng(args.seed + 7).standard_normal((n, k)), device=dev)
+    X = torch.zeros_like(B)
+    b1 = B[:, 0].contiguous()
+    x1 = torch.zeros_like(b1)
+    rr = np.zeros(k)
+    it = np.zeros(k, dtype=np.int32)
+    stream = torch.cuda.current_stream(dev)
+    st = stream.cuda_stream
+
+    def solve(b, x, kk):
+        _lib.check(L.rchol_gpu_pcg_d(Ad.ptr, F.ptr, b.data_ptr(), x.data_ptr(), kk, args.tol, args.maxit,
+                                     _lib.pd(rr), it.ctypes.data_as(_lib._ip), st))
+
+    t1 = _event_ms(torch, lambda: solve(b1, x1, 1), 3, stream)
+    it1 = int(it[0])
+    tk = _event_ms(torch, lambda: solve(B, X, k), 2, stream)
+    Xh = X.cpu().numpy()
+    Bh = B.cpu().numpy()
+    perm, _ = tree.arrays()
+    Ap = A[perm][:, perm].tocsr()
+    worst = float(max(np.linalg.norm(Ap @ Xh[:, j] - Bh[:, j]) / np.linalg.norm(Bh[:, j]) for j in range(k)))
+    return {"workload": "PCG to 1e-8, 7-point constant Laplacian 128^3 (n=2,097,152), 32 right-hand sides, FP32 G",
+            "ms_single_rhs": round(t1, 2), "iters_single": it1, "ms_32_rhs": round(tk, 2),
+            "iters_32": [int(it.min()), int(it.max())], "relres_host_fp64_worst": worst,
+            "per_rhs_throughput_vs_single": round(t1 * k / tk, 2)}
+
+
+def run_batched(args, dev):
+    """512 independent 2D 5-point Dirichlet grids, side ~ U{32..256}, edge
+    weights exp(0.5 N(0,1)), one N(0,1) right-hand side each, PCG to 1e-8 with
+    a block-diagonal FP32 G: all systems in the same launches, against the
+    same systems solved one at a time (a sample of 16, extrapolated)."""
+    import torch
+
+    import rchol_gb300 as R
+    from rchol_gb300 import generators
+
+    rng = np.random.default_rng(args.seed + 11)
+    sides = rng.integers(32, 257, 512)
+    mats = [generators.grid_2d_weighted(int(sd), int(sd), "lognormal", sigma=0.5, rng=rng) for sd in sides]
+    bs = [rng.standard_normal(A.shape[0]) for A in mats]
+    t0 = time.time()
+    Bt = R.Batch(mats, threads=4, seed=args.seed, precision=R.PREC_FP32)
+    torch.cuda.synchronize(dev)
+    setup = time.time() - t0
+    Bt.solve(bs, args.tol, args.maxit)
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        xs, relres, itr = Bt.solve(bs, args.tol, args.maxit)
+        times.append(time.perf_counter() - t0)
+    tb = min(times) * 1e3
+    worst = float(max(np.linalg.norm(mats[s] @ xs[s] - bs[s]) / np.linalg.norm(bs[s]) for s in range(len(mats))))
+    samp = list(range(0, len(mats), len(mats) // 16))
+    tot = 0.0
+    for s in samp:
+        G, perm, part = R.rchol(mats[s], 4, seed=args.seed, precision="fp32")
+        Aps = mats[s][perm][:, perm]
+        R.pcg(Aps, bs[s][perm], args.tol, args.maxit, G)
+        t0 = time.perf_counter()
+        R.pcg(Aps, bs[s][perm], args.tol, args.maxit, G)
+        tot += time.perf_counter() - t0
+    one = tot / len(samp) * 1e3
+    return {"workload": "512 2D 5-point Dirichlet grids, side U{32..256} (n=%d), log-normal(0.5) weights, "
+                        "PCG to 1e-8, block-diagonal FP32 G, host buffers" % int(Bt.sys_ptr[-1]),
+            "ms_all_systems": round(tb, 1), "iters": [int(itr.min()), int(itr.max())],
+            "relres_host_fp64_worst": worst, "setup_s": round(setup, 1),
+            "ms_per_system_one_at_a_time": round(one, 2),
+            "speedup_vs_one_at_a_time": round(one * len(mats) / tb, 1)}
 
 
 def cpu_baseline(args, Ap, bp, F64, it64):

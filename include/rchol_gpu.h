@@ -60,6 +60,15 @@ int64_t rchol_gpu_launch_count(void);
  * entries, the last one counting the ground vertex). */
 int rchol_gpu_tree_build(int64_t n, const int64_t *row_ptr, const int64_t *col_idx,
                          int threads, rchol_tree_t *out);
+/* Many independent systems at once (no counterpart in the reference, which
+ * orders one matrix per call): the matrix is block diagonal with system s on
+ * rows [sys_ptr[s], sys_ptr[s+1]).  Each system is ordered like
+ * rchol_gpu_tree_build with `threads` leaves and keeps its row range under
+ * the permutation; the systems' trees hang below empty separators of one
+ * tree, so the factor of the whole matrix is block diagonal. */
+int rchol_gpu_tree_build_batch(int64_t nsys, const int64_t *sys_ptr, int64_t n,
+                               const int64_t *row_ptr, const int64_t *col_idx, int threads,
+                               rchol_tree_t *out);
 /* Reuse a stored ordering (python/rchol/rchol.py:24-34). */
 int rchol_gpu_tree_from_partition(int64_t n, const int64_t *perm, const int64_t *part,
                                   int64_t nparts, rchol_tree_t *out);
@@ -124,6 +133,19 @@ int rchol_gpu_pcg(rchol_matrix_t A, rchol_factor_t G, const double *b, double *x
 int rchol_gpu_pcg_d(rchol_matrix_t A, rchol_factor_t G, const double *d_b, double *d_x,
                     int64_t nrhs, double tol, int maxit, double *relres, int *itr,
                     void *stream);
+/* Independent PCG solves (c++/util/pcg.cpp:57-127 per system) of the
+ * diagonal blocks of A, system s on the (permuted) rows [sys_ptr[s],
+ * sys_ptr[s+1]), with a block-diagonal G (a factor of a matrix ordered by
+ * rchol_gpu_tree_build_batch).  Every system has its own scalars, stopping
+ * test and iteration count; relres and itr have nsys entries.  One SpMV and
+ * one preconditioner apply per iteration serve all systems.  No counterpart
+ * in the reference. */
+int rchol_gpu_pcg_batch(rchol_matrix_t A, rchol_factor_t G, int64_t nsys, const int64_t *sys_ptr,
+                        const double *b, double *x, double tol, int maxit, double *relres,
+                        int *itr);
+int rchol_gpu_pcg_batch_d(rchol_matrix_t A, rchol_factor_t G, int64_t nsys,
+                          const int64_t *sys_ptr, const double *d_b, double *d_x, double tol,
+                          int maxit, double *relres, int *itr, void *stream);
 /* z = (G G^T)^-1 r (c++/util/pcg.cpp:141-159); device pointers. */
 int rchol_gpu_precond_d(rchol_factor_t G, const double *d_r, double *d_z, int64_t nrhs,
                         void *stream);

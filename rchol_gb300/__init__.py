@@ -24,10 +24,11 @@ import scipy.sparse as sp
 
 from . import _lib
 from ._lib import PREC_FP32, PREC_FP64, Factor, Matrix, RcholError, Tree
+from .batch import Batch
 from .generators import (checkerboard_3d, grid_2d_weighted, laplace_3d, laplace_3d_weighted,
                          sddm_to_laplacian)
 
-__all__ = ["rchol", "pcg", "Solver", "Tree", "Matrix", "Factor", "RcholError", "laplace_3d",
+__all__ = ["rchol", "pcg", "Solver", "Batch", "Tree", "Matrix", "Factor", "RcholError", "laplace_3d",
            "laplace_3d_weighted", "grid_2d_weighted", "checkerboard_3d", "sddm_to_laplacian",
            "PREC_FP64", "PREC_FP32", "precision_code"]
 

@@ -29,6 +29,7 @@ SIGNATURES = [
     ("rchol_gpu_version", C.c_char_p, []),
     ("rchol_gpu_launch_count", _i64, []),
     ("rchol_gpu_tree_build", C.c_int, [_i64, _i64p, _i64p, C.c_int, C.POINTER(_vp)]),
+    ("rchol_gpu_tree_build_batch", C.c_int, [_i64, _i64p, _i64, _i64p, _i64p, C.c_int, C.POINTER(_vp)]),
     ("rchol_gpu_tree_from_partition", C.c_int, [_i64, _i64p, _i64p, _i64, C.POINTER(_vp)]),
     ("rchol_gpu_tree_size", _i64, [_vp]),
     ("rchol_gpu_tree_num_parts", _i64, [_vp]),
@@ -50,6 +51,8 @@ SIGNATURES = [
     ("rchol_gpu_factor_destroy", None, [_vp]),
     ("rchol_gpu_pcg", C.c_int, [_vp, _vp, _dp, _dp, _i64, C.c_double, C.c_int, _dp, _ip]),
     ("rchol_gpu_pcg_d", C.c_int, [_vp, _vp, _vp, _vp, _i64, C.c_double, C.c_int, _dp, _ip, _vp]),
+    ("rchol_gpu_pcg_batch", C.c_int, [_vp, _vp, _i64, _i64p, _dp, _dp, C.c_double, C.c_int, _dp, _ip]),
+    ("rchol_gpu_pcg_batch_d", C.c_int, [_vp, _vp, _i64, _i64p, _vp, _vp, C.c_double, C.c_int, _dp, _ip, _vp]),
     ("rchol_gpu_precond_d", C.c_int, [_vp, _vp, _vp, _i64, _vp]),
     ("rchol_gpu_precond_noalloc_d", C.c_int, [_vp, _vp, _vp, _vp]),
     ("rchol_gpu_trsv_d", C.c_int, [_vp, C.c_int, _vp, _vp, _i64, _vp]),
@@ -135,6 +138,16 @@ class Tree(Handle):
         rp, ci = i64(rowptr), i64(colidx)
         out = _vp()
         check(lib().rchol_gpu_tree_build(len(rp) - 1, p64(rp), p64(ci), int(threads), C.byref(out)))
+        return cls(out)
+
+    @classmethod
+    def build_batch(cls, sys_ptr, rowptr, colidx, threads):
+        """Block-diagonal matrix of independent systems (rows sys_ptr[s] ..
+        sys_ptr[s+1]), each ordered on its own; see rchol_gpu_tree_build_batch."""
+        sp, rp, ci = i64(sys_ptr), i64(rowptr), i64(colidx)
+        out = _vp()
+        check(lib().rchol_gpu_tree_build_batch(len(sp) - 1, p64(sp), len(rp) - 1, p64(rp), p64(ci), int(threads),
+                                               C.byref(out)))
         return cls(out)
 
     @classmethod

@@ -29,6 +29,11 @@ void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *
 void pcg_host(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x, int k,
               double tol, int maxit, double *relres, int *itr);
 int64_t plan_levels(const rchol_factor_s &F, bool upper);
+void pcg_batch_device(const rchol_matrix_s &A, const rchol_factor_s &F, int64_t nseg, const int64_t *seg,
+                      const double *b, double *x, double tol, int maxit, double *relres, int *itr,
+                      cudaStream_t s);
+void pcg_batch_host(const rchol_matrix_s &A, const rchol_factor_s &F, int64_t nseg, const int64_t *seg,
+                    const double *b, double *x, double tol, int maxit, double *relres, int *itr);
 void edge_grad(int64_t m, const int64_t *ei, const int64_t *ej, const double *lam, const double *x, double *g,
                cudaStream_t s);
 void precond_noalloc(const rchol_factor_s &F, const double *r, double *z, cudaStream_t s);
@@ -70,6 +75,15 @@ int rchol_gpu_tree_build(int64_t n, const int64_t *row_ptr, const int64_t *col_i
   RCHOL_CHECK_ARG(out, "null output handle");
   *out = nullptr;
   *out = build_tree(n, row_ptr, col_idx, threads);
+  API_END
+}
+
+int rchol_gpu_tree_build_batch(int64_t nsys, const int64_t *sys_ptr, int64_t n, const int64_t *row_ptr,
+                               const int64_t *col_idx, int threads, rchol_tree_t *out) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(out, "null output handle");
+  *out = nullptr;
+  *out = build_tree_batch(nsys, sys_ptr, n, row_ptr, col_idx, threads);
   API_END
 }
 
@@ -276,6 +290,36 @@ int rchol_gpu_pcg(rchol_matrix_t A, rchol_factor_t G, const double *b, double *x
   RCHOL_CHECK_ARG(A->n == G->n, "matrix and factor sizes differ");
   RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   pcg_host(*A, *G, b, x, (int)nrhs, tol, maxit, relres, itr);
+  API_END
+}
+
+static void check_systems(rchol_matrix_t A, int64_t nsys, const int64_t *sys_ptr) {
+  RCHOL_CHECK_ARG(nsys >= 1 && sys_ptr, "need at least one system");
+  RCHOL_CHECK_ARG(sys_ptr[0] == 0 && sys_ptr[nsys] == A->n, "system offsets must run from 0 to n");
+  for (int64_t s = 0; s < nsys; ++s)
+    RCHOL_CHECK_ARG(sys_ptr[s + 1] > sys_ptr[s], "every system needs at least one row");
+}
+
+int rchol_gpu_pcg_batch_d(rchol_matrix_t A, rchol_factor_t G, int64_t nsys, const int64_t *sys_ptr,
+                          const double *d_b, double *d_x, double tol, int maxit, double *relres, int *itr,
+                          void *stream) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(A && G && d_b && d_x && relres && itr, "null argument");
+  RCHOL_CHECK_ARG(A->n == G->n, "matrix and factor sizes differ");
+  RCHOL_CHECK_ARG(maxit >= 0, "maxit must be nonnegative");
+  check_systems(A, nsys, sys_ptr);
+  pcg_batch_device(*A, *G, nsys, sys_ptr, d_b, d_x, tol, maxit, relres, itr, as_stream(stream));
+  API_END
+}
+
+int rchol_gpu_pcg_batch(rchol_matrix_t A, rchol_factor_t G, int64_t nsys, const int64_t *sys_ptr,
+                        const double *b, double *x, double tol, int maxit, double *relres, int *itr) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(A && G && b && x && relres && itr, "null argument");
+  RCHOL_CHECK_ARG(A->n == G->n, "matrix and factor sizes differ");
+  RCHOL_CHECK_ARG(maxit >= 0, "maxit must be nonnegative");
+  check_systems(A, nsys, sys_ptr);
+  pcg_batch_host(*A, *G, nsys, sys_ptr, b, x, tol, maxit, relres, itr);
   API_END
 }
 

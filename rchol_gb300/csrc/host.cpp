@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <memory>
 #include <future>
 #include <numeric>
 #include <thread>
@@ -308,6 +309,76 @@ rchol_tree_s *tree_from_partition(int64_t n, const int64_t *perm, const int64_t 
   t->part.assign(part, part + nparts);
   build_nodes(*t);
   return t;
+}
+
+// Many independent systems as one block-diagonal matrix: every system is
+// ordered on its own (the same nested dissection as build_tree, `threads`
+// leaves each), and the per-system trees become the subtrees of one complete
+// binary tree whose upper separators are empty.  The system count is padded
+// to a power of two with empty systems, so the union has the post-order
+// result_idx layout of a single ordering with nsys_pad * threads leaves.  The
+// ground vertex sits in the (otherwise empty) root separator; no elimination
+// creates an edge between two systems, so G is block diagonal.  Each system
+// keeps its rows [sys_ptr[s], sys_ptr[s+1]) under the permutation.
+rchol_tree_s *build_tree_batch(int64_t nsys, const int64_t *sys_ptr, int64_t n, const int64_t *rp,
+                               const int64_t *ci, int threads) {
+  RCHOL_CHECK_ARG(nsys >= 1 && sys_ptr, "need at least one system");
+  RCHOL_CHECK_ARG(threads > 0 && (threads & (threads - 1)) == 0, "thread number should be a power of 2");
+  RCHOL_CHECK_ARG(sys_ptr[0] == 0 && sys_ptr[nsys] == n, "system offsets must run from 0 to n");
+  for (int64_t s = 0; s < nsys; ++s)
+    RCHOL_CHECK_ARG(sys_ptr[s + 1] > sys_ptr[s], "every system needs at least one row");
+  validate_csr(n, rp, ci);
+  for (int64_t s = 0; s < nsys; ++s)
+    for (int64_t i = sys_ptr[s]; i < sys_ptr[s + 1]; ++i)
+      for (int64_t q = rp[i]; q < rp[i + 1]; ++q)
+        RCHOL_CHECK_ARG(ci[q] >= sys_ptr[s] && ci[q] < sys_ptr[s + 1],
+                        "the matrix must be block diagonal over the systems");
+  int64_t pad = 1;
+  while (pad < nsys) pad *= 2;
+  const int64_t segs_sys = 2 * (int64_t)threads - 1;
+  std::vector<std::vector<int64_t>> part_sys(nsys);  // segment sizes per system
+  auto t = new rchol_tree_s();
+  try {
+    t->n = n;
+    t->perm.resize(n);
+    for (int64_t s = 0; s < nsys; ++s) {
+      const int64_t b = sys_ptr[s], ns = sys_ptr[s + 1] - b;
+      std::vector<int64_t> lrp(ns + 1), lci;
+      lci.reserve(rp[sys_ptr[s + 1]] - rp[b]);
+      for (int64_t i = 0; i < ns; ++i) {
+        for (int64_t q = rp[b + i]; q < rp[b + i + 1]; ++q) lci.push_back(ci[q] - b);
+        lrp[i + 1] = (int64_t)lci.size();
+      }
+      std::unique_ptr<rchol_tree_s> ts(build_tree(ns, lrp.data(), lci.data(), threads));
+      for (int64_t i = 0; i < ns; ++i) t->perm[b + i] = ts->perm[i] + b;
+      std::vector<int64_t> &sz = part_sys[s];
+      sz.resize(segs_sys);
+      for (int64_t j = 0; j < segs_sys; ++j) sz[j] = ts->part[j + 1] - ts->part[j];
+      sz.back() -= 1;  // the system's own ground slot; the union has one ground
+    }
+    // post-order of the complete tree over padded systems
+    std::vector<int64_t> sizes;
+    std::function<void(int64_t, int64_t)> rec = [&](int64_t s0, int64_t cnt) {
+      if (cnt == 1) {
+        if (s0 < nsys) sizes.insert(sizes.end(), part_sys[s0].begin(), part_sys[s0].end());
+        else sizes.insert(sizes.end(), segs_sys, 0);
+        return;
+      }
+      rec(s0, cnt / 2);
+      rec(s0 + cnt / 2, cnt / 2);
+      sizes.push_back(0);  // empty separator joining the two halves
+    };
+    rec(0, pad);
+    t->threads = (int)(pad * threads);
+    t->part.assign(1, 0);
+    for (int64_t x : sizes) t->part.push_back(t->part.back() + x);
+    t->part.back() += 1;  // ground vertex in the root separator
+    build_nodes(*t);
+    return t;
+  } catch (...) {
+    delete t;
+    throw;
+  }
 }
 
 // c++/util/util.cpp:16-49: B = A(p,p) with each row's columns sorted.

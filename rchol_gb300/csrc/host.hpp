@@ -15,6 +15,8 @@ void validate_csr(int64_t n, const int64_t *rp, const int64_t *ci);
 rchol_tree_s *build_tree(int64_t n, const int64_t *rp, const int64_t *ci, int threads);
 rchol_tree_s *tree_from_partition(int64_t n, const int64_t *perm, const int64_t *part,
                                   int64_t nparts);
+rchol_tree_s *build_tree_batch(int64_t nsys, const int64_t *sys_ptr, int64_t n, const int64_t *rp,
+                               const int64_t *ci, int threads);
 // B = A(perm, perm); srcpos[q] = position in A of B's entry q.
 HostCsr reorder(int64_t n, const int64_t *rp, const int64_t *ci, const double *v,
                 const std::vector<int64_t> &perm, std::vector<int64_t> *srcpos = nullptr);

@@ -89,9 +89,32 @@ struct PcgWork {
   }
 };
 
+// Workspace and captured graph of the batched PCG: independent systems that
+// are the diagonal blocks (row ranges seg[s] .. seg[s+1]) of one matrix.
+struct SegWork {
+  uint64_t key_uid = 0;
+  std::vector<int64_t> seg_host;
+  int64_t n = 0;
+  DevBuf<int64_t> seg;
+  DevBuf<double> r, z, p, q, x, sc;
+  DevBuf<double> hb, hx;
+  DevBuf<int> ic;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t graph_kernels = 0;
+  ~SegWork() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
 struct SolvePlan {
   std::mutex lock;  // solves on one factor are serialised (they share workspaces)
   std::vector<std::unique_ptr<PcgWork>> pcg;
+  std::vector<std::unique_ptr<SegWork>> seg;
   DirPlan fwd, bwd;
   StreamDir sfwd, sbwd;
   StreamDir kfwd, kbwd;    // pieces for up to 32 right-hand sides (built on first use)

@@ -727,7 +727,10 @@ static void ensure_scratch(SolvePlan &P, bool fp32, int64_t count) {
     if (P.scratch.n < (size_t)count) P.scratch.alloc(count), grew = true;
     if (P.ytmp.n < (size_t)count) P.ytmp.alloc(count), grew = true;
   }
-  if (grew) P.pcg.clear();
+  if (grew) {
+    P.pcg.clear();
+    P.seg.clear();
+  }
 }
 
 // The preconditioner with the plan's buffers already sized (inside PCG).
@@ -973,6 +976,277 @@ void pcg_device(const rchol_matrix_s &A, const rchol_factor_s &F, const double *
 void pcg_host(const rchol_matrix_s &A, const rchol_factor_s &F, const double *b, double *x, int k, double tol,
               int maxit, double *relres, int *itr) {
   pcg_impl(A, F, nullptr, nullptr, b, x, k, tol, maxit, relres, itr, 0);
+}
+
+// ---- batched PCG over independent systems ---------------------------------------------
+//
+// The systems are the diagonal blocks of one matrix (rows seg[s] .. seg[s+1])
+// with a block-diagonal factor, so one SpMV and one preconditioner apply serve
+// them all; the scalars of c++/util/pcg.cpp:57-127 are kept per system, one
+// thread block per system computes them (fixed reduction trees, so results
+// are deterministic), and a system stops updating once it has converged.
+
+namespace {
+
+constexpr int SEG_THREADS = 256;
+
+struct SegState {
+  const int64_t *seg;
+  int nseg;
+  double *bnorm2, *rz, *rz_prev, *relres;
+  int *active, *iters, *any_active;
+  const double *tol;
+  const int *maxit;
+};
+
+// Block-wide sum in a fixed tree; every thread gets the total.
+__device__ double seg_sum(double v, double *sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int h = SEG_THREADS / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  const double t = sh[0];
+  __syncthreads();
+  return t;
+}
+
+// x = 0, r = b, ||b||^2 and the first stopping test (pcg.cpp:60-70).
+__global__ void __launch_bounds__(SEG_THREADS) seg_init_kernel(SegState st, const double *b, double *x,
+                                                               double *r) {
+  __shared__ double sh[SEG_THREADS];
+  const int s = blockIdx.x;
+  const int64_t i0 = st.seg[s], i1 = st.seg[s + 1];
+  double acc = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += SEG_THREADS) {
+    const double bv = b[i];
+    x[i] = 0.0;
+    r[i] = bv;
+    acc += bv * bv;
+  }
+  const double t = seg_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    st.bnorm2[s] = t;
+    st.iters[s] = 0;
+    const int act = (sqrt(t) > sqrt(t) * *st.tol) && (*st.maxit > 0);
+    st.active[s] = act;
+    if (act) atomicOr(st.any_active, 1);
+  }
+}
+
+// rz = r.z, beta = rz / rz_prev, p = z (first iteration) or beta p + z.
+__global__ void __launch_bounds__(SEG_THREADS) seg_beta_kernel(SegState st, const double *r, const double *z,
+                                                               double *p) {
+  __shared__ double sh[SEG_THREADS];
+  if (!*st.any_active) return;
+  const int s = blockIdx.x;
+  if (!st.active[s]) return;
+  const int64_t i0 = st.seg[s], i1 = st.seg[s + 1];
+  double acc = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += SEG_THREADS) acc += r[i] * z[i];
+  const double rz = seg_sum(acc, sh);
+  const int it = st.iters[s];
+  const double beta = it == 0 ? 0.0 : rz / st.rz_prev[s];
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += SEG_THREADS) p[i] = it == 0 ? z[i] : beta * p[i] + 1.0 * z[i];
+  if (threadIdx.x == 0) st.rz[s] = rz;
+}
+
+// alpha = p.r / p.q, x += alpha p, r -= alpha q, then the stopping test.
+__global__ void __launch_bounds__(SEG_THREADS) seg_alpha_kernel(SegState st, const double *p, const double *q,
+                                                                double *x, double *r) {
+  __shared__ double sh[SEG_THREADS];
+  if (!*st.any_active) return;
+  const int s = blockIdx.x;
+  if (!st.active[s]) return;
+  const int64_t i0 = st.seg[s], i1 = st.seg[s + 1];
+  double a0 = 0.0, a1 = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += SEG_THREADS) {
+    const double pv = p[i];
+    a0 += pv * q[i];
+    a1 += pv * r[i];
+  }
+  const double pq = seg_sum(a0, sh);
+  const double pr = seg_sum(a1, sh);
+  const double alpha = pr / pq;
+  double rr = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += SEG_THREADS) {
+    x[i] += alpha * p[i];
+    const double rv = r[i] + -alpha * q[i];
+    r[i] = rv;
+    rr += rv * rv;
+  }
+  const double t = seg_sum(rr, sh);
+  if (threadIdx.x == 0) {
+    const int it = st.iters[s] + 1;
+    st.iters[s] = it;
+    st.rz_prev[s] = st.rz[s];
+    st.active[s] = (sqrt(t) > sqrt(st.bnorm2[s]) * *st.tol) && (it < *st.maxit);
+  }
+}
+
+__global__ void seg_any_kernel(SegState st) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  int a = 0;
+  for (int s = threadIdx.x; s < st.nseg; s += blockDim.x) a |= st.active[s];
+  if (a) atomicOr(&any, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) *st.any_active = any;
+}
+
+// relres = ||A x - b|| / ||b|| per system (q = A x).
+__global__ void __launch_bounds__(SEG_THREADS) seg_resid_kernel(SegState st, const double *q, const double *b) {
+  __shared__ double sh[SEG_THREADS];
+  const int s = blockIdx.x;
+  const int64_t i0 = st.seg[s], i1 = st.seg[s + 1];
+  double acc = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += SEG_THREADS) {
+    const double d = q[i] + -1.0 * b[i];
+    acc += d * d;
+  }
+  const double t = seg_sum(acc, sh);
+  if (threadIdx.x == 0) st.relres[s] = sqrt(t) / sqrt(st.bnorm2[s]);
+}
+
+}  // namespace
+
+static SegWork &seg_workspace(const rchol_matrix_s &A, const rchol_factor_s &F, int64_t nseg,
+                              const int64_t *seg) {
+  SolvePlan &P = *F.plan;
+  for (auto &w : P.seg)
+    if (w->key_uid == A.uid && (int64_t)w->seg_host.size() == nseg + 1 &&
+        std::equal(w->seg_host.begin(), w->seg_host.end(), seg))
+      return *w;
+  if (P.seg.size() >= 4) P.seg.erase(P.seg.begin());
+  auto w = std::make_unique<SegWork>();
+  w->key_uid = A.uid;
+  w->seg_host.assign(seg, seg + nseg + 1);
+  w->n = A.n;
+  w->seg.upload(seg, nseg + 1, 0);
+  w->r.alloc(A.n);
+  w->z.alloc(A.n);
+  w->p.alloc(A.n);
+  w->q.alloc(A.n);
+  w->x.alloc(A.n);
+  w->sc.alloc(4 * (size_t)nseg + 1);
+  w->ic.alloc(2 * (size_t)nseg + 2);
+  RCHOL_CUDA(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+  RCHOL_CUDA(cudaEventCreateWithFlags(&w->ev_in, cudaEventDisableTiming));
+  RCHOL_CUDA(cudaEventCreateWithFlags(&w->ev_out, cudaEventDisableTiming));
+  RCHOL_CUDA(cudaStreamSynchronize(0));
+  P.seg.push_back(std::move(w));
+  return *P.seg.back();
+}
+
+static SegState seg_state(SegWork &w) {
+  const int S = (int)(w.seg_host.size() - 1);
+  SegState st;
+  st.seg = w.seg.p;
+  st.nseg = S;
+  st.bnorm2 = w.sc.p;
+  st.rz = w.sc.p + S;
+  st.rz_prev = w.sc.p + 2 * (size_t)S;
+  st.relres = w.sc.p + 3 * (size_t)S;
+  st.tol = w.sc.p + 4 * (size_t)S;
+  st.active = w.ic.p;
+  st.iters = w.ic.p + S;
+  st.any_active = w.ic.p + 2 * (size_t)S;
+  st.maxit = w.ic.p + 2 * (size_t)S + 1;
+  return st;
+}
+
+static void pcg_batch_impl(const rchol_matrix_s &A, const rchol_factor_s &F, int64_t nseg, const int64_t *seg,
+                           const double *b, double *x, const double *b_host, double *x_host, double tol,
+                           int maxit, double *relres, int *itr, cudaStream_t s) {
+  SolvePlan &P = *F.plan;
+  std::lock_guard<std::mutex> guard(P.lock);
+  const int64_t n = A.n;
+  const bool fp32 = F.precision == RCHOL_PREC_FP32;
+  ensure_scratch(P, fp32, n);
+  if (fp32 ? P.acc32.n < (size_t)n : P.acc64.n < (size_t)n) {
+    if (fp32) P.acc32.alloc(n);
+    else P.acc64.alloc(n);
+  }
+  SegWork &w = seg_workspace(A, F, nseg, seg);
+  SegState st = seg_state(w);
+  const unsigned S = (unsigned)nseg;
+  cudaStream_t ws = w.stream;
+  RCHOL_CUDA(cudaEventRecord(w.ev_in, s));
+  RCHOL_CUDA(cudaStreamWaitEvent(ws, w.ev_in, 0));
+  if (b_host) {
+    if (w.hb.n < (size_t)n) w.hb.alloc(n);
+    if (w.hx.n < (size_t)n) w.hx.alloc(n);
+    RCHOL_CUDA(cudaMemcpyAsync(w.hb.p, b_host, n * sizeof(double), cudaMemcpyHostToDevice, ws));
+    b = w.hb.p;
+    x = w.hx.p;
+  }
+  if (!w.exec) {
+    cudaGraph_t g = nullptr;
+    RCHOL_CUDA(cudaStreamBeginCapture(ws, cudaStreamCaptureModeThreadLocal));
+    try {
+      precond_ready(F, w.r.p, w.z.p, 1, ws);
+      seg_beta_kernel<<<S, SEG_THREADS, 0, ws>>>(st, w.r.p, w.z.p, w.p.p);
+      spmv(A, w.p.p, w.q.p, 1, ws);
+      seg_alpha_kernel<<<S, SEG_THREADS, 0, ws>>>(st, w.p.p, w.q.p, w.x.p, w.r.p);
+      seg_any_kernel<<<1, 256, 0, ws>>>(st);
+      RCHOL_CUDA(cudaGetLastError());
+    } catch (...) {
+      cudaStreamEndCapture(ws, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    RCHOL_CUDA(cudaStreamEndCapture(ws, &g));
+    size_t nodes = 0;
+    RCHOL_CUDA(cudaGraphGetNodes(g, nullptr, &nodes));
+    w.graph_kernels = (int64_t)nodes;
+    cudaError_t e = cudaGraphInstantiate(&w.exec, g, 0);
+    cudaGraphDestroy(g);
+    RCHOL_CUDA(e);
+  }
+  double htol = tol;
+  int hmax = maxit;
+  RCHOL_CUDA(cudaMemsetAsync(w.sc.p, 0, w.sc.bytes(), ws));
+  RCHOL_CUDA(cudaMemsetAsync(w.ic.p, 0, w.ic.bytes(), ws));
+  RCHOL_CUDA(cudaMemcpyAsync(const_cast<double *>(st.tol), &htol, sizeof(double), cudaMemcpyHostToDevice, ws));
+  RCHOL_CUDA(cudaMemcpyAsync(const_cast<int *>(st.maxit), &hmax, sizeof(int), cudaMemcpyHostToDevice, ws));
+  seg_init_kernel<<<S, SEG_THREADS, 0, ws>>>(st, b, w.x.p, w.r.p);
+  note_launch(1);
+  RCHOL_CUDA(cudaGetLastError());
+  int h_any = 1;
+  for (int it = 0; it < maxit;) {
+    const int batch = it == 0 ? 8 : 4;
+    for (int j = 0; j < batch && it < maxit; ++j, ++it) {
+      RCHOL_CUDA(cudaGraphLaunch(w.exec, ws));
+      note_launch(w.graph_kernels);
+    }
+    RCHOL_CUDA(cudaMemcpyAsync(&h_any, st.any_active, sizeof(int), cudaMemcpyDeviceToHost, ws));
+    RCHOL_CUDA(cudaStreamSynchronize(ws));
+    if (!h_any) break;
+  }
+  spmv(A, w.x.p, w.q.p, 1, ws);
+  seg_resid_kernel<<<S, SEG_THREADS, 0, ws>>>(st, w.q.p, b);
+  note_launch(2);
+  RCHOL_CUDA(cudaGetLastError());
+  if (x_host) RCHOL_CUDA(cudaMemcpyAsync(x_host, w.x.p, n * sizeof(double), cudaMemcpyDeviceToHost, ws));
+  else RCHOL_CUDA(cudaMemcpyAsync(x, w.x.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ws));
+  RCHOL_CUDA(cudaMemcpyAsync(relres, st.relres, nseg * sizeof(double), cudaMemcpyDeviceToHost, ws));
+  RCHOL_CUDA(cudaMemcpyAsync(itr, st.iters, nseg * sizeof(int), cudaMemcpyDeviceToHost, ws));
+  RCHOL_CUDA(cudaEventRecord(w.ev_out, ws));
+  RCHOL_CUDA(cudaStreamWaitEvent(s, w.ev_out, 0));
+  RCHOL_CUDA(cudaStreamSynchronize(ws));
+}
+
+void pcg_batch_device(const rchol_matrix_s &A, const rchol_factor_s &F, int64_t nseg, const int64_t *seg,
+                      const double *b, double *x, double tol, int maxit, double *relres, int *itr,
+                      cudaStream_t s) {
+  pcg_batch_impl(A, F, nseg, seg, b, x, nullptr, nullptr, tol, maxit, relres, itr, s);
+}
+
+void pcg_batch_host(const rchol_matrix_s &A, const rchol_factor_s &F, int64_t nseg, const int64_t *seg,
+                    const double *b, double *x, double tol, int maxit, double *relres, int *itr) {
+  pcg_batch_impl(A, F, nseg, seg, nullptr, nullptr, b, x, tol, maxit, relres, itr, 0);
 }
 
 }  // namespace rchol

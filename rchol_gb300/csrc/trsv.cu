@@ -325,6 +325,32 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// Byte ranges of a piece's records, read one record ahead: records are
+// fetched in order, so the global-memory latency of the offsets overlaps a
+// whole step instead of sitting in front of every fetch.
+struct OffsetPipe {
+  const int64_t *off;  // off[0 .. n]
+  int n, k;
+  int64_t beg, end, nxt;
+  __device__ __forceinline__ void init(const int64_t *o, int nrec) {
+    off = o;
+    n = nrec;
+    k = 0;
+    beg = o[0];
+    end = nrec >= 1 ? o[1] : beg;
+    nxt = nrec >= 2 ? o[2] : end;
+  }
+  // range of record k (the next one), then advance
+  __device__ __forceinline__ void next(int64_t &b, int64_t &e) {
+    b = beg;
+    e = end;
+    ++k;
+    beg = end;
+    end = nxt;
+    nxt = k + 2 <= n ? off[k + 2] : end;
+  }
+};
+
 #ifdef RCHOL_DEVICE_CHECKS
 // Diagnostic build only: bounds checks report the first violations and skip
 // the access (uniform conditions make the whole warp leave).
@@ -398,10 +424,13 @@ __global__ void __launch_bounds__(128) block_kernel(BlockArgs<VT> a, OutT *out) 
   const int64_t *boff = a.blk_off + nd.blk0;
 
   // ring of nbuf block buffers; block k lives in slot k % nbuf
-  auto load = [&](int k) {
+  OffsetPipe op;
+  op.init(boff, nd.nblocks);
+  auto load = [&](int k) {  // called for k = 0, 1, 2, ... in order
     unsigned char *dst = base + (size_t)(k % nbuf) * a.bufbytes;
-    const int64_t o0 = boff[k];
-    int64_t len = boff[k + 1] - o0;
+    int64_t o0, o1;
+    op.next(o0, o1);
+    int64_t len = o1 - o0;
 #ifdef RCHOL_DEVICE_CHECKS
     if (len < 0 || len > a.bufbytes || (o0 & 15)) {
       if (lane == 0) dbg_report("block record length", len, a.bufbytes);
@@ -608,10 +637,14 @@ __global__ void __launch_bounds__(512) team_kernel(TeamArgs<VT> a, OutT *out) {
   const int64_t *boff = a.blk_off + nd.blk0;
   const int nb = nd.nblocks;
 
-  auto load = [&](int k, int slot) {  // helpers only; one commit group per record (empty past the end)
+  OffsetPipe op;
+  op.init(boff, nb);
+  auto load = [&](int k, int slot) {  // helpers only, k in order; one commit group per record (empty past the end)
     if (k < nb) {
       unsigned char *dst = ring + (size_t)slot * a.bufbytes;
-      const int64_t o0 = boff[k], len = boff[k + 1] - o0;
+      int64_t o0, o1;
+      op.next(o0, o1);
+      const int64_t len = o1 - o0;
       for (int64_t o = (int64_t)ht * 16; o < len; o += (int64_t)TH * 16) cp_async16(dst + o, src + o0 + o);
     }
     cp_async_commit();
@@ -750,10 +783,14 @@ __global__ void __launch_bounds__(256) team_k_kernel(TeamArgs<VT> a, OutT *out, 
   const int64_t *boff = a.blk_off + nd.blk0;
   const int nb = nd.nblocks;
 
-  auto load = [&](int b) {
+  OffsetPipe op;
+  op.init(boff, nb);
+  auto load = [&](int b) {  // b in order
     if (b < nb) {
       unsigned char *dst = ring + (size_t)(b % RING) * a.bufbytes;
-      const int64_t o0 = boff[b], len = boff[b + 1] - o0;
+      int64_t o0, o1;
+      op.next(o0, o1);
+      const int64_t len = o1 - o0;
       for (int64_t o = (int64_t)ht * 16; o < len; o += (int64_t)TH * 16) cp_async16(dst + o, src + o0 + o);
     }
     cp_async_commit();
