@@ -18,10 +18,52 @@ from . import _lib
 from ._lib import PREC_FP32, Factor, Matrix, Tree
 
 
+def autotune_threads(mats, candidates=(1, 2, 4, 8, 16), sample=8, seed=0, precision=PREC_FP32, reps=3):
+    """Leaves per system (the ``threads`` of Batch) chosen by measurement: the
+    largest ``sample`` systems are factored with every candidate and the
+    preconditioner apply (the dominant cost of a PCG iteration) is timed on
+    the GPU with CUDA events; the fastest candidate wins.  Returns
+    (best, {candidate: ms})."""
+    import torch
+
+    mats = list(mats)
+    order = np.argsort([-A.shape[0] for A in mats])[: max(1, sample)]
+    probe = [mats[i] for i in order]
+    timings = {}
+    stream = torch.cuda.current_stream()
+    for t in candidates:
+        if min(A.shape[0] for A in probe) < 4 * t:
+            continue
+        b = Batch(probe, threads=t, seed=seed, precision=precision)
+        n = int(b.sys_ptr[-1])
+        d_r = torch.as_tensor(np.random.default_rng(seed).standard_normal(n), device="cuda")
+        d_z = torch.empty_like(d_r)
+
+        def apply():
+            _lib.check(_lib.lib().rchol_gpu_precond_d(b.F.ptr, d_r.data_ptr(), d_z.data_ptr(), 1,
+                                                      stream.cuda_stream))
+
+        apply()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            apply()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        timings[t] = e0.elapsed_time(e1) / reps
+        del b
+    return min(timings, key=timings.get), timings
+
+
 class Batch:
-    """Factor of a list of SDDM matrices (scipy.sparse, any sizes)."""
+    """Factor of a list of SDDM matrices (scipy.sparse, any sizes).  With
+    ``threads=0`` the leaves per system are chosen by autotune_threads."""
 
     def __init__(self, mats, threads=4, seed=0, precision=PREC_FP32, G=None):
+        if threads == 0:
+            threads, self.tuning = autotune_threads(mats, seed=seed, precision=precision)
+        self.threads = threads
         mats = [sp.csr_matrix(A) for A in mats]
         for A in mats:
             A.sum_duplicates()

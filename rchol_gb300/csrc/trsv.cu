@@ -164,48 +164,52 @@ void build_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
 }
 
 // Team format.  A thread block of W warps solves the piece: warp 0 (the
-// solver) retires one block per step, while the W-1 helper warps sum, for the
-// block after it, the entries whose columns lie in blocks older than the one
-// being solved ("far" entries), in chunks of near-equal length.  The solver
-// then only adds the previous block's entries ("near") and the chunk sums of
-// its row before applying the inverse.  Record (16-byte aligned sections):
-//   u32 hdr[16]  nrows, row0, prev_row0, nnear, nchunk, nfar, col_bytes, 0,
-//                then the byte offsets of near_col, near_val, chunk_row,
-//                chunk_beg, far_col, far_val, minv and near_off
-//   u16 near_off[33]       lane r's near entries [near_off[r], near_off[r+1])
+// solver) retires one block per step, while the W-1 helper warps prepare the
+// block after it: they sum the entries whose columns lie in blocks older than
+// the one being solved ("far" entries) in chunks of equal length, one chunk
+// per helper thread, reduce the chunks of every row and leave
+// u_r = acc_r - far_r for the solver.  The solver adds the previous block's
+// entries ("near") with shuffles of the previous block's solution, which it
+// still holds in registers, and applies the inverse.  Record (16-byte aligned
+// sections):
+//   u32 hdr[16]  nrows, row0, prev_row0, nnear, nchunk, chunk_len, col_bytes,
+//                most near entries of one row, then the byte offsets of
+//                near_col, near_val, chunk_row, far_col, far_val, minv, near_off
+//   u16 near_off[33]       row r's near entries [near_off[r], near_off[r+1])
 //   u8  near_col[nnear]    column inside the previous block (0..31)
 //   VT  near_val[nnear]
 //   u16 chunk_row[33]      row r's chunks [chunk_row[r], chunk_row[r+1])
-//   u32 chunk_beg[nchunk+1] chunk c = far entries [chunk_beg[c], chunk_beg[c+1])
-//   u16|u32 far_col[nfar]  piece-local columns
-//   VT  far_val[nfar]
+//   u16|u32 far_col[chunk_len][nchunk]  entry j of chunk c at j * nchunk + c
+//   VT  far_val[chunk_len][nchunk]      (padding: column 0, value 0)
 //   VT  minv[528]          as in the warp format
+// Interleaving the chunks makes the helpers' loads of one step contiguous.
 struct TeamLayout {
-  size_t o_noff, o_ncol, o_nval, o_crow, o_cbeg, o_fcol, o_fval, o_min, len;
+  size_t o_noff, o_ncol, o_nval, o_crow, o_fcol, o_fval, o_min, len;
 };
 
-__host__ __device__ inline TeamLayout team_layout(uint32_t nnear, uint32_t nchunk, uint32_t nfar, uint32_t csz,
+__host__ __device__ inline TeamLayout team_layout(uint32_t nnear, uint32_t nchunk, uint32_t clen, uint32_t csz,
                                                   uint32_t vsz) {
   TeamLayout L;
   L.o_noff = 64;
   L.o_ncol = L.o_noff + al16(2 * (BS + 1));
   L.o_nval = L.o_ncol + al16(nnear);
   L.o_crow = L.o_nval + al16((size_t)vsz * nnear);
-  L.o_cbeg = L.o_crow + al16(2 * (BS + 1));
-  L.o_fcol = L.o_cbeg + al16(4 * ((size_t)nchunk + 1));
-  L.o_fval = L.o_fcol + al16((size_t)csz * nfar);
-  L.o_min = L.o_fval + al16((size_t)vsz * nfar);
+  L.o_fcol = L.o_crow + al16(2 * (BS + 1));
+  L.o_fval = L.o_fcol + al16((size_t)csz * nchunk * clen);
+  L.o_min = L.o_fval + al16((size_t)vsz * nchunk * clen);
   L.len = L.o_min + al16((size_t)vsz * TRI);
   return L;
 }
 
 // Upper bound of a team record whose block has `cnt` entries in earlier
 // blocks of its piece (near and far entries together), for helpers of
-// `helper_threads` threads.
+// `helper_threads` threads: chunks of len ceil(cnt / helper_threads) pad at
+// most one chunk per row.
 inline size_t team_record_bound(size_t cnt, size_t helper_threads, size_t vsz, size_t csz) {
-  const size_t chunks = std::min(cnt, helper_threads + BS);
-  return 64 + 2 * al16(2 * (BS + 1)) + al16(std::min<size_t>(cnt, BS * BS)) + al16(4 * (chunks + 1)) +
-         al16(csz * cnt) + vsz * cnt + 32 + al16(vsz * TRI);
+  const size_t clen = std::max<size_t>(1, (cnt + helper_threads - 1) / helper_threads);
+  const size_t padded = cnt + BS * clen;
+  return 64 + 2 * al16(2 * (BS + 1)) + al16(std::min<size_t>(cnt, BS * BS)) + al16(vsz * std::min<size_t>(cnt, BS * BS)) +
+         al16(csz * padded) + al16(vsz * padded) + al16(vsz * TRI);
 }
 
 void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, const std::vector<double> &v,
@@ -249,27 +253,26 @@ void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
       }
     }
     invert_block(T, upper, X);
-    // balanced chunks over the helper threads; a chunk never spans two rows
-    const uint32_t target = std::max<uint32_t>(4, (nfar + helper_threads - 1) / std::max(1, helper_threads));
+    // chunks of clen entries (the last one of a row padded), about one per
+    // helper thread; a chunk never spans two rows
+    const uint32_t clen = std::max<uint32_t>(1, (nfar + helper_threads - 1) / std::max(1, helper_threads));
     uint16_t crow[BS + 1];
-    std::vector<uint32_t> cbeg(1, 0);
     crow[0] = 0;
+    uint32_t nchunk = 0, nmax = 0;
     for (int r = 0; r < BS; ++r) {
-      const uint32_t m = (uint32_t)farl[r].size();
-      const uint32_t nc = (m + target - 1) / target, start = cbeg.back();
-      for (uint32_t j = 1; j <= nc; ++j) cbeg.push_back(start + (uint32_t)(j * (uint64_t)m / nc));
-      crow[r + 1] = (uint16_t)(cbeg.size() - 1);
+      nchunk += ((uint32_t)farl[r].size() + clen - 1) / clen;
+      crow[r + 1] = (uint16_t)nchunk;
+      nmax = std::max<uint32_t>(nmax, (uint32_t)nearl[r].size());
     }
-    const uint32_t nchunk = (uint32_t)cbeg.size() - 1;
     maxchunk = std::max<int32_t>(maxchunk, (int32_t)nchunk);
-    const TeamLayout L = team_layout(nnear, nchunk, nfar, csz, (uint32_t)vsz);
+    const TeamLayout L = team_layout(nnear, nchunk, clen, csz, (uint32_t)vsz);
     const size_t base = P.bytes.size();
     P.bytes.resize(base + L.len, 0);
     unsigned char *p = P.bytes.data() + base;
-    const uint32_t hdr[16] = {(uint32_t)nr,     (uint32_t)row0,   (uint32_t)prow0,  nnear,
-                              nchunk,           nfar,             csz,              0,
-                              (uint32_t)L.o_ncol, (uint32_t)L.o_nval, (uint32_t)L.o_crow, (uint32_t)L.o_cbeg,
-                              (uint32_t)L.o_fcol, (uint32_t)L.o_fval, (uint32_t)L.o_min,  (uint32_t)L.o_noff};
+    const uint32_t hdr[16] = {(uint32_t)nr,       (uint32_t)row0,     (uint32_t)prow0,    nnear,
+                              nchunk,             clen,               csz,                nmax,
+                              (uint32_t)L.o_ncol, (uint32_t)L.o_nval, (uint32_t)L.o_crow, (uint32_t)L.o_fcol,
+                              (uint32_t)L.o_fval, (uint32_t)L.o_min,  (uint32_t)L.o_noff, 0};
     std::memcpy(p, hdr, sizeof(hdr));
     auto put_val = [&](size_t off, size_t idx, double x) {
       if (vsz == 8) std::memcpy(p + off + 8 * idx, &x, 8);
@@ -280,7 +283,7 @@ void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
     };
     uint16_t noff[BS + 1];
     noff[0] = 0;
-    size_t w = 0, wf = 0;
+    size_t w = 0;
     for (int r = 0; r < BS; ++r) {
       for (auto &en : nearl[r]) {
         p[L.o_ncol + w] = (unsigned char)en.first;
@@ -288,20 +291,19 @@ void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
         ++w;
       }
       noff[r + 1] = (uint16_t)w;
-      for (auto &en : farl[r]) {
+      for (size_t q = 0; q < farl[r].size(); ++q) {  // entry q of row r: chunk crow[r] + q / clen, slot q % clen
+        const size_t at = (size_t)(q % clen) * nchunk + crow[r] + q / clen;
         if (csz == 2) {
-          const uint16_t c16 = (uint16_t)en.first;
-          std::memcpy(p + L.o_fcol + 2 * wf, &c16, 2);
+          const uint16_t c16 = (uint16_t)farl[r][q].first;
+          std::memcpy(p + L.o_fcol + 2 * at, &c16, 2);
         } else {
-          std::memcpy(p + L.o_fcol + 4 * wf, &en.first, 4);
+          std::memcpy(p + L.o_fcol + 4 * at, &farl[r][q].first, 4);
         }
-        put_val(L.o_fval, wf, en.second);
-        ++wf;
+        put_val(L.o_fval, at, farl[r][q].second);
       }
     }
     std::memcpy(p + L.o_noff, noff, sizeof(noff));
     std::memcpy(p + L.o_crow, crow, sizeof(crow));
-    std::memcpy(p + L.o_cbeg, cbeg.data(), 4 * cbeg.size());
     for (int c = 0; c < BS; ++c) {
       const int r_lo = upper ? 0 : c, r_hi = upper ? c : BS - 1;
       for (int r = r_lo; r <= r_hi; ++r)
@@ -324,32 +326,6 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
-
-// Byte ranges of a piece's records, read one record ahead: records are
-// fetched in order, so the global-memory latency of the offsets overlaps a
-// whole step instead of sitting in front of every fetch.
-struct OffsetPipe {
-  const int64_t *off;  // off[0 .. n]
-  int n, k;
-  int64_t beg, end, nxt;
-  __device__ __forceinline__ void init(const int64_t *o, int nrec) {
-    off = o;
-    n = nrec;
-    k = 0;
-    beg = o[0];
-    end = nrec >= 1 ? o[1] : beg;
-    nxt = nrec >= 2 ? o[2] : end;
-  }
-  // range of record k (the next one), then advance
-  __device__ __forceinline__ void next(int64_t &b, int64_t &e) {
-    b = beg;
-    e = end;
-    ++k;
-    beg = end;
-    end = nxt;
-    nxt = k + 2 <= n ? off[k + 2] : end;
-  }
-};
 
 #ifdef RCHOL_DEVICE_CHECKS
 // Diagnostic build only: bounds checks report the first violations and skip
@@ -424,13 +400,10 @@ __global__ void __launch_bounds__(128) block_kernel(BlockArgs<VT> a, OutT *out) 
   const int64_t *boff = a.blk_off + nd.blk0;
 
   // ring of nbuf block buffers; block k lives in slot k % nbuf
-  OffsetPipe op;
-  op.init(boff, nd.nblocks);
-  auto load = [&](int k) {  // called for k = 0, 1, 2, ... in order
+  auto load = [&](int k) {
     unsigned char *dst = base + (size_t)(k % nbuf) * a.bufbytes;
-    int64_t o0, o1;
-    op.next(o0, o1);
-    int64_t len = o1 - o0;
+    const int64_t o0 = boff[k];
+    int64_t len = boff[k + 1] - o0;
 #ifdef RCHOL_DEVICE_CHECKS
     if (len < 0 || len > a.bufbytes || (o0 & 15)) {
       if (lane == 0) dbg_report("block record length", len, a.bufbytes);
@@ -568,7 +541,7 @@ struct TeamArgs {
   int node0;            // first piece of the stage; piece = node0 + blockIdx.x
   int bufbytes;         // per-record buffer (16-aligned)
   int ring;             // records in the ring (4..8): the solved block's, the next one's, ring-2 in flight
-  int maxchunk;         // chunk sums per parity buffer
+  int maxchunk;         // most chunks of one block (chunk-sum buffer)
   const unsigned char *blocks;
   const int64_t *blk_off;
   const VT *acc;
@@ -589,27 +562,10 @@ __device__ __forceinline__ void cp_async_wait_upto(int n) {
   }
 }
 
-// sum_{e in [e0, e1)} val[e] * x[col[e]] with four independent chains (the
-// column loads of four entries are issued before their gathers).
-template <typename VT, typename CT>
-__device__ __forceinline__ VT chunk_sum(const CT *col, const VT *val, const VT *x, uint32_t e0, uint32_t e1) {
-  VT s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-  uint32_t e = e0;
-  for (; e + 3 < e1; e += 4) {
-    const uint32_t c0 = col[e], c1 = col[e + 1], c2 = col[e + 2], c3 = col[e + 3];
-    s0 += val[e] * x[c0];
-    s1 += val[e + 1] * x[c1];
-    s2 += val[e + 2] * x[c2];
-    s3 += val[e + 3] * x[c3];
-  }
-  for (; e < e1; ++e) s0 += val[e] * x[col[e]];
-  return (s0 + s1) + (s2 + s3);
-}
-
 // Header of a team record, read with four 16-byte loads.
 struct TeamHdr {
-  uint32_t nr, row0, prow0, nnear, nchunk, nfar, csz, pad;
-  uint32_t o_ncol, o_nval, o_crow, o_cbeg, o_fcol, o_fval, o_min, o_noff;
+  uint32_t nr, row0, prow0, nnear, nchunk, clen, csz, nmax;
+  uint32_t o_ncol, o_nval, o_crow, o_fcol, o_fval, o_min, o_noff, pad;
 };
 
 __device__ __forceinline__ TeamHdr read_hdr(const unsigned char *p) {
@@ -618,33 +574,52 @@ __device__ __forceinline__ TeamHdr read_hdr(const unsigned char *p) {
   return TeamHdr{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
 }
 
-// One thread block per piece: warp 0 solves, the other warps sum far entries
-// one block ahead and stream the records in.  One barrier per block.  The
-// solver's step is a latency chain, so everything that does not depend on
-// the previous block (the header, the lane's row of the inverse, its own
-// right-hand side and chunk sums) is loaded before the near entries.
+// Sum of chunk c: clen entries interleaved with stride nchunk.
+template <typename VT, typename CT>
+__device__ __forceinline__ VT chunk_sum(const CT *col, const VT *val, const VT *x, uint32_t c, uint32_t nchunk,
+                                        uint32_t clen) {
+  VT s0 = 0, s1 = 0;
+  uint32_t j = 0, at = c;
+  for (; j + 1 < clen; j += 2, at += 2 * nchunk) {
+    s0 += val[at] * x[col[at]];
+    s1 += val[at + nchunk] * x[col[at + nchunk]];
+  }
+  if (j < clen) s0 += val[at] * x[col[at]];
+  return s0 + s1;
+}
+
+// Named barrier of the helper warps only (the solver does not take part).
+__device__ __forceinline__ void helpers_sync(int nthreads) {
+  asm volatile("bar.sync 1, %0;\n" ::"r"(nthreads) : "memory");
+}
+
+// One thread block per piece.  Per step k (one __syncthreads):
+//   warp 0   t = u_k - near_k . x_{k-1} (shuffles of the previous block's
+//            solution, kept in registers), x_k = T_k^-1 t (shuffles);
+//   helpers  chunk sums of block k+1 (columns solved before block k), then
+//            warp 1 folds them per row into u_{k+1} = acc - far; all helper
+//            threads stream record k+RING-1 into the ring.
+// The solver's chain per step is therefore only shuffles and FMAs; every
+// load it issues is independent of the previous block.
 template <typename VT, typename OutT, bool UPPER>
-__global__ void __launch_bounds__(512) team_kernel(TeamArgs<VT> a, OutT *out) {
+__global__ void __launch_bounds__(256, 2) team_kernel(TeamArgs<VT> a, OutT *out) {
   extern __shared__ __align__(16) unsigned char smem[];
   const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ht = tid - 32, TH = (int)blockDim.x - 32;  // helper thread index / count
   unsigned char *ring = smem;
   const int RING = a.ring;
-  VT *part = reinterpret_cast<VT *>(smem + (size_t)RING * a.bufbytes);
-  VT *xs = reinterpret_cast<VT *>(reinterpret_cast<unsigned char *>(part) + al16(2 * (size_t)a.maxchunk * sizeof(VT)));
+  VT *part = reinterpret_cast<VT *>(smem + (size_t)RING * a.bufbytes);  // chunk sums of the next block
+  VT *ubuf = reinterpret_cast<VT *>(reinterpret_cast<unsigned char *>(part) + al16((size_t)a.maxchunk * sizeof(VT)));
+  VT *xs = ubuf + 2 * BS;  // u of blocks k and k+1 (parity), then the piece's unknowns
   const unsigned char *src = a.blocks;
   const int64_t *boff = a.blk_off + nd.blk0;
   const int nb = nd.nblocks;
 
-  OffsetPipe op;
-  op.init(boff, nb);
-  auto load = [&](int k, int slot) {  // helpers only, k in order; one commit group per record (empty past the end)
+  auto load = [&](int k, int slot) {  // helpers only; one commit group per record (empty past the end)
     if (k < nb) {
       unsigned char *dst = ring + (size_t)slot * a.bufbytes;
-      int64_t o0, o1;
-      op.next(o0, o1);
-      const int64_t len = o1 - o0;
+      const int64_t o0 = boff[k], len = boff[k + 1] - o0;
       for (int64_t o = (int64_t)ht * 16; o < len; o += (int64_t)TH * 16) cp_async16(dst + o, src + o0 + o);
     }
     cp_async_commit();
@@ -656,6 +631,7 @@ __global__ void __launch_bounds__(512) team_kernel(TeamArgs<VT> a, OutT *out) {
   }
   __syncthreads();
 
+  VT xprev = 0;  // solver: x of the previous block, lane c = its row c
   int slot = 0;  // ring slot of record k
   for (int k = 0; k < nb; ++k) {
     const int next = slot + 1 == RING ? 0 : slot + 1;
@@ -671,57 +647,60 @@ __global__ void __launch_bounds__(512) team_kernel(TeamArgs<VT> a, OutT *out) {
         m[c] = minv[in ? tri_col_off(c, UPPER) + (UPPER ? lane : lane - c) : 0];
         m[c] = in ? m[c] : VT(0);
       }
-      VT t = 0;
-      if (lane < (int)h.nr) {
-        const uint16_t *noff = reinterpret_cast<const uint16_t *>(p + h.o_noff);
-        const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h.o_crow);
-        const VT *pk = part + (size_t)(k & 1) * a.maxchunk;
-        const VT own = xs[h.row0 + lane];
-        VT s1 = 0, s3 = 0;
-        uint32_t c = crow[lane];
-        const uint32_t c1 = crow[lane + 1];
-        for (; c + 1 < c1; c += 2) {
-          s1 += pk[c];
-          s3 += pk[c + 1];
-        }
-        if (c < c1) s1 += pk[c];
-        s1 += s3;
-        const unsigned char *ncol = p + h.o_ncol;
-        const VT *nval = reinterpret_cast<const VT *>(p + h.o_nval);
-        const VT *xp = xs + h.prow0;
-        VT s0 = 0, s2 = 0;
-        uint32_t e = noff[lane];
-        const uint32_t e1 = noff[lane + 1];
-        for (; e + 3 < e1; e += 4) {
-          const unsigned c0 = ncol[e], c1 = ncol[e + 1], c2 = ncol[e + 2], c3 = ncol[e + 3];
-          s0 += nval[e] * xp[c0];
-          s2 += nval[e + 1] * xp[c1];
-          s0 += nval[e + 2] * xp[c2];
-          s2 += nval[e + 3] * xp[c3];
-        }
-        for (; e < e1; ++e) s0 += nval[e] * xp[ncol[e]];
-        t = own - ((s0 + s2) + s1);
+      const bool row = lane < (int)h.nr;
+      // u = acc - far (block 0 has no far entries)
+      const VT u = !row ? VT(0) : k == 0 ? xs[h.row0 + lane] : ubuf[(k & 1) * BS + lane];
+      const uint16_t *noff = reinterpret_cast<const uint16_t *>(p + h.o_noff);
+      const unsigned char *ncol = p + h.o_ncol;
+      const VT *nval = reinterpret_cast<const VT *>(p + h.o_nval);
+      const uint32_t e0 = noff[lane], cnt = row ? noff[lane + 1] - e0 : 0;
+      VT s0 = 0, s1 = 0;
+      uint32_t j = 0;
+      for (; j + 1 < h.nmax; j += 2) {  // uniform trip count: every lane takes part in the shuffles
+        const bool ok0 = j < cnt, ok1 = j + 1 < cnt;
+        const int c0 = ok0 ? ncol[e0 + j] : 0, c1 = ok1 ? ncol[e0 + j + 1] : 0;
+        const VT v0 = ok0 ? nval[e0 + j] : VT(0), v1 = ok1 ? nval[e0 + j + 1] : VT(0);
+        s0 += v0 * __shfl_sync(0xffffffffu, xprev, c0);
+        s1 += v1 * __shfl_sync(0xffffffffu, xprev, c1);
       }
-      VT c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+      if (j < h.nmax) {
+        const bool ok0 = j < cnt;
+        const int c0 = ok0 ? ncol[e0 + j] : 0;
+        const VT v0 = ok0 ? nval[e0 + j] : VT(0);
+        s0 += v0 * __shfl_sync(0xffffffffu, xprev, c0);
+      }
+      const VT t = u - (s0 + s1);
+      VT d0 = 0, d1 = 0, d2 = 0, d3 = 0;
 #pragma unroll
       for (int c = 0; c < BS; c += 4) {
-        c0 += m[c + 0] * __shfl_sync(0xffffffffu, t, c + 0);
-        c1 += m[c + 1] * __shfl_sync(0xffffffffu, t, c + 1);
-        c2 += m[c + 2] * __shfl_sync(0xffffffffu, t, c + 2);
-        c3 += m[c + 3] * __shfl_sync(0xffffffffu, t, c + 3);
+        d0 += m[c + 0] * __shfl_sync(0xffffffffu, t, c + 0);
+        d1 += m[c + 1] * __shfl_sync(0xffffffffu, t, c + 1);
+        d2 += m[c + 2] * __shfl_sync(0xffffffffu, t, c + 2);
+        d3 += m[c + 3] * __shfl_sync(0xffffffffu, t, c + 3);
       }
-      if (lane < (int)h.nr) xs[h.row0 + lane] = (c0 + c1) + (c2 + c3);
+      const VT x = (d0 + d1) + (d2 + d3);
+      if (row) xs[h.row0 + lane] = x;
+      xprev = x;
     } else {
-      if (k + 1 < nb) {  // far sums of block k+1: columns in blocks solved before block k
+      if (k + 1 < nb) {  // block k+1: far sums (columns solved before block k), then u per row
         const unsigned char *p = ring + (size_t)next * a.bufbytes;
         const TeamHdr h = read_hdr(p);
-        const uint32_t *cbeg = reinterpret_cast<const uint32_t *>(p + h.o_cbeg);
         const VT *fval = reinterpret_cast<const VT *>(p + h.o_fval);
-        VT *pk = part + (size_t)((k + 1) & 1) * a.maxchunk;
-        for (int c = ht; c < (int)h.nchunk; c += TH) {
-          const uint32_t e0 = cbeg[c], e1 = cbeg[c + 1];
-          pk[c] = h.csz == 2 ? chunk_sum(reinterpret_cast<const uint16_t *>(p + h.o_fcol), fval, xs, e0, e1)
-                             : chunk_sum(reinterpret_cast<const uint32_t *>(p + h.o_fcol), fval, xs, e0, e1);
+        for (int c = ht; c < (int)h.nchunk; c += TH)
+          part[c] = h.csz == 2 ? chunk_sum(reinterpret_cast<const uint16_t *>(p + h.o_fcol), fval, xs, c, h.nchunk, h.clen)
+                               : chunk_sum(reinterpret_cast<const uint32_t *>(p + h.o_fcol), fval, xs, c, h.nchunk, h.clen);
+        helpers_sync(TH);
+        if (ht < BS) {
+          const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h.o_crow);
+          VT f0 = 0, f1 = 0;
+          uint32_t c = crow[ht];
+          const uint32_t c1 = crow[ht + 1];
+          for (; c + 1 < c1; c += 2) {
+            f0 += part[c];
+            f1 += part[c + 1];
+          }
+          if (c < c1) f0 += part[c];
+          ubuf[((k + 1) & 1) * BS + ht] = ht < (int)h.nr ? xs[h.row0 + ht] - (f0 + f1) : VT(0);
         }
       }
       // record k+RING-1 goes into the slot of record k-1, retired last step
@@ -770,7 +749,7 @@ __global__ void __launch_bounds__(256) ext_k_kernel(const int32_t *__restrict__ 
 // registers); helper warps sum the far entries of block b+1 row by row into
 // part[(b+1)&1][row][lane] and stream the records.  One barrier per block.
 template <typename VT, typename OutT, bool UPPER>
-__global__ void __launch_bounds__(256) team_k_kernel(TeamArgs<VT> a, OutT *out, int k, int64_t ld) {
+__global__ void __launch_bounds__(256, 1) team_k_kernel(TeamArgs<VT> a, OutT *out, int k, int64_t ld) {
   extern __shared__ __align__(16) unsigned char smem[];
   const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -783,14 +762,10 @@ __global__ void __launch_bounds__(256) team_k_kernel(TeamArgs<VT> a, OutT *out, 
   const int64_t *boff = a.blk_off + nd.blk0;
   const int nb = nd.nblocks;
 
-  OffsetPipe op;
-  op.init(boff, nb);
-  auto load = [&](int b) {  // b in order
+  auto load = [&](int b) {
     if (b < nb) {
       unsigned char *dst = ring + (size_t)(b % RING) * a.bufbytes;
-      int64_t o0, o1;
-      op.next(o0, o1);
-      const int64_t len = o1 - o0;
+      const int64_t o0 = boff[b], len = boff[b + 1] - o0;
       for (int64_t o = (int64_t)ht * 16; o < len; o += (int64_t)TH * 16) cp_async16(dst + o, src + o0 + o);
     }
     cp_async_commit();
@@ -845,27 +820,27 @@ __global__ void __launch_bounds__(256) team_k_kernel(TeamArgs<VT> a, OutT *out, 
         const TeamHdr h = read_hdr(p);
         const uint32_t csz = h.csz;
         const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h.o_crow);
-        const uint32_t *cbeg = reinterpret_cast<const uint32_t *>(p + h.o_cbeg);
         const VT *fval = reinterpret_cast<const VT *>(p + h.o_fval);
         VT *pb = part + (size_t)((b + 1) & 1) * BS * KW;
+        const uint32_t nch = h.nchunk, clen = h.clen;
         for (int r = warp - 1; r < BS; r += HW) {
           VT s0 = 0, s1 = 0;
-          uint32_t e = cbeg[crow[r]];
-          const uint32_t e1 = cbeg[crow[r + 1]];
-          if (csz == 2) {
-            const uint16_t *col = reinterpret_cast<const uint16_t *>(p + h.o_fcol);
-            for (; e + 1 < e1; e += 2) {
-              s0 += fval[e] * xs[col[e] * KW + lane];
-              s1 += fval[e + 1] * xs[col[e + 1] * KW + lane];
+          for (uint32_t c = crow[r]; c < crow[r + 1]; ++c) {  // the row's chunks, entries strided by nchunk
+            if (csz == 2) {
+              const uint16_t *col = reinterpret_cast<const uint16_t *>(p + h.o_fcol);
+              for (uint32_t j = 0, at = c; j < clen; ++j, at += nch) {
+                const VT v = fval[at] * xs[col[at] * KW + lane];
+                if (j & 1) s1 += v;
+                else s0 += v;
+              }
+            } else {
+              const uint32_t *col = reinterpret_cast<const uint32_t *>(p + h.o_fcol);
+              for (uint32_t j = 0, at = c; j < clen; ++j, at += nch) {
+                const VT v = fval[at] * xs[(size_t)col[at] * KW + lane];
+                if (j & 1) s1 += v;
+                else s0 += v;
+              }
             }
-            if (e < e1) s0 += fval[e] * xs[col[e] * KW + lane];
-          } else {
-            const uint32_t *col = reinterpret_cast<const uint32_t *>(p + h.o_fcol);
-            for (; e + 1 < e1; e += 2) {
-              s0 += fval[e] * xs[(size_t)col[e] * KW + lane];
-              s1 += fval[e + 1] * xs[(size_t)col[e + 1] * KW + lane];
-            }
-            if (e < e1) s0 += fval[e] * xs[(size_t)col[e] * KW + lane];
           }
           pb[r * KW + lane] = s0 + s1;
         }
@@ -1136,10 +1111,10 @@ static void build_streams_width(const rchol_factor_s &F, int kwidth, StreamDir &
   // Schedule knobs (tuning only; every setting solves exactly the same
   // system): RCHOL_TRSV_TEAM = 0 warp format everywhere, 1 team format for
   // separators, 2 team format everywhere (default); RCHOL_TRSV_TEAM_WARPS =
-  // warps of a team (2..16, default 8).
+  // warps of a team (2..8, default 8).
   int team_mode = 2, team_warps = 8;
   if (const char *e = getenv("RCHOL_TRSV_TEAM")) team_mode = std::max(0, std::min(2, atoi(e)));
-  if (const char *e = getenv("RCHOL_TRSV_TEAM_WARPS")) team_warps = std::max(2, std::min(16, atoi(e)));
+  if (const char *e = getenv("RCHOL_TRSV_TEAM_WARPS")) team_warps = std::max(2, std::min(8, atoi(e)));
   if (kwidth > 1) team_warps = 8;
   fwd.team_warps = bwd.team_warps = team_warps;
   build_dir_streams(rp, ci, v, n, F.nodes, false, fp32, team_mode, kwidth, fwd, s);
@@ -1234,7 +1209,7 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       ta.node0 = D.stage_ptr[st];
       ta.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
       ta.maxchunk = D.stage_chunks[st];
-      const size_t fixed = al16(2 * (size_t)ta.maxchunk * sizeof(VT)) + xs_bytes;
+      const size_t fixed = al16((size_t)ta.maxchunk * sizeof(VT)) + 2 * BS * sizeof(VT) + xs_bytes;
       // the deepest ring that fits (records arrive ring-3 steps ahead of use)
       // where few pieces share the GPU; where many do, they hide each
       // other's latency and shared memory goes to residency instead

@@ -124,3 +124,21 @@ def test_batch_pcg_matches_per_system_reference(cuda, R, O, precision):
         # the reported residual is the true one
         true = np.linalg.norm(A @ xs[s] - bs[s]) / np.linalg.norm(bs[s])
         assert abs(true - relres[s]) <= 1e-10, s
+
+
+@pytest.mark.gpu
+def test_batch_autotuned_leaves(cuda, R):
+    """threads=0 picks the leaves per system by timing the preconditioner on
+    the largest systems; the chosen setting solves every system."""
+    from rchol_gb300.batch import autotune_threads
+
+    mats = _systems()
+    best, timings = autotune_threads(mats, candidates=(1, 2, 4), sample=3)
+    assert best in timings and all(v > 0 for v in timings.values())
+    B = R.Batch(mats, threads=0)
+    assert B.threads in timings
+    rng = np.random.default_rng(2)
+    bs = [rng.standard_normal(A.shape[0]) for A in mats]
+    xs, relres, itr = B.solve(bs, tol=1e-8, maxit=200)
+    for s, A in enumerate(mats):
+        assert np.linalg.norm(A @ xs[s] - bs[s]) <= 1.5e-8 * np.linalg.norm(bs[s])
