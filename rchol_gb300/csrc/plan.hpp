@@ -41,6 +41,7 @@ struct StreamDir {
   std::vector<int> stage_maxrec;     // largest block record of the stage (bytes)
   std::vector<int64_t> stage_row_ptr;  // rows of split stages: srows[stage_row_ptr[s] ..]
   std::vector<int> stage_team;       // 1: team format (a thread block per piece)
+  std::vector<int> stage_warps;      // team format: warps of the stage's teams
   std::vector<int> stage_chunks;     // team format: most chunks of one block in the stage
   std::vector<int> stage_ext_lanes;  // lanes per row of the external prologue (1, 4, 8 or 32)
   int team_warps = 8;                // warps of a team (1 solver + helpers)

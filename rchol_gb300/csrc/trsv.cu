@@ -173,11 +173,15 @@ void build_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
 // still holds in registers, and applies the inverse.  Record (16-byte aligned
 // sections):
 //   u32 hdr[16]  nrows, row0, prev_row0, nnear, nchunk, chunk_len, col_bytes,
-//                most near entries of one row, then the byte offsets of
-//                near_col, near_val, chunk_row, far_col, far_val, minv, near_off
-//   u16 near_off[33]       row r's near entries [near_off[r], near_off[r+1])
-//   u8  near_col[nnear]    column inside the previous block (0..31)
-//   VT  near_val[nnear]
+//                nmax (most near entries of one row), then the byte offsets
+//                of near_col, near_val, chunk_row, far_col, far_val, minv,
+//                near_off
+//   near entries, column inside the previous block (0..31) and value, either
+//     rows in turn (single right-hand side):
+//       u16 near_off[33]; u8 near_col[nnear]; VT near_val[nnear]
+//     or slot-major for the 32-wide solve, entry j of row r at j * 32 + r
+//     (padding: column 0, value 0):
+//       u8 near_col[nmax][32]; VT near_val[nmax][32]
 //   u16 chunk_row[33]      row r's chunks [chunk_row[r], chunk_row[r+1])
 //   u16|u32 far_col[chunk_len][nchunk]  entry j of chunk c at j * nchunk + c
 //   VT  far_val[chunk_len][nchunk]      (padding: column 0, value 0)
@@ -187,13 +191,15 @@ struct TeamLayout {
   size_t o_noff, o_ncol, o_nval, o_crow, o_fcol, o_fval, o_min, len;
 };
 
-__host__ __device__ inline TeamLayout team_layout(uint32_t nnear, uint32_t nchunk, uint32_t clen, uint32_t csz,
-                                                  uint32_t vsz) {
+// nnear: near entries; slots: nmax for the slot-major layout, 0 for rows in turn.
+__host__ __device__ inline TeamLayout team_layout(uint32_t nnear, uint32_t slots, uint32_t nchunk, uint32_t clen,
+                                                  uint32_t csz, uint32_t vsz) {
   TeamLayout L;
+  const size_t nent = slots ? (size_t)BS * slots : nnear;
   L.o_noff = 64;
-  L.o_ncol = L.o_noff + al16(2 * (BS + 1));
-  L.o_nval = L.o_ncol + al16(nnear);
-  L.o_crow = L.o_nval + al16((size_t)vsz * nnear);
+  L.o_ncol = slots ? 64 : 64 + al16(2 * (BS + 1));
+  L.o_nval = L.o_ncol + al16(nent);
+  L.o_crow = L.o_nval + al16((size_t)vsz * nent);
   L.o_fcol = L.o_crow + al16(2 * (BS + 1));
   L.o_fval = L.o_fcol + al16((size_t)csz * nchunk * clen);
   L.o_min = L.o_fval + al16((size_t)vsz * nchunk * clen);
@@ -206,15 +212,17 @@ __host__ __device__ inline TeamLayout team_layout(uint32_t nnear, uint32_t nchun
 // `helper_threads` threads: chunks of len ceil(cnt / helper_threads) pad at
 // most one chunk per row.
 inline size_t team_record_bound(size_t cnt, size_t helper_threads, size_t vsz, size_t csz) {
-  const size_t clen = std::max<size_t>(1, (cnt + helper_threads - 1) / helper_threads);
+  const size_t slots = helper_threads > (size_t)BS ? helper_threads - BS : 1;
+  const size_t clen = std::max<size_t>(1, (cnt + slots - 1) / slots);
   const size_t padded = cnt + BS * clen;
-  return 64 + 2 * al16(2 * (BS + 1)) + al16(std::min<size_t>(cnt, BS * BS)) + al16(vsz * std::min<size_t>(cnt, BS * BS)) +
-         al16(csz * padded) + al16(vsz * padded) + al16(vsz * TRI);
+  const size_t near = (size_t)BS * std::min<size_t>(cnt, BS);  // either layout: at most 32 x min(cnt, 32)
+  return 64 + al16(2 * (BS + 1)) + al16(near) + al16(vsz * near) + al16(2 * (BS + 1)) + al16(csz * padded) +
+         al16(vsz * padded) + al16(vsz * TRI);
 }
 
 void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, const std::vector<double> &v,
-                      int64_t b, int64_t e, bool upper, size_t vsz, int helper_threads, PieceBuild &P,
-                      int32_t &maxchunk) {
+                      int64_t b, int64_t e, bool upper, size_t vsz, int helper_threads, bool slot_major,
+                      PieceBuild &P, int32_t &maxchunk) {
   const int64_t R = e - b, nb = (R + BS - 1) / BS;
   const uint32_t csz = R > 65535 ? 4 : 2;
   P.offs.assign(1, 0);
@@ -253,9 +261,11 @@ void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
       }
     }
     invert_block(T, upper, X);
-    // chunks of clen entries (the last one of a row padded), about one per
-    // helper thread; a chunk never spans two rows
-    const uint32_t clen = std::max<uint32_t>(1, (nfar + helper_threads - 1) / std::max(1, helper_threads));
+    // chunks of clen entries (the last one of a row padded), at most one per
+    // helper thread (each row adds at most one partial chunk); a chunk never
+    // spans two rows
+    const int slots = std::max(1, helper_threads - BS);
+    const uint32_t clen = std::max<uint32_t>(1, (nfar + slots - 1) / slots);
     uint16_t crow[BS + 1];
     crow[0] = 0;
     uint32_t nchunk = 0, nmax = 0;
@@ -265,7 +275,7 @@ void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
       nmax = std::max<uint32_t>(nmax, (uint32_t)nearl[r].size());
     }
     maxchunk = std::max<int32_t>(maxchunk, (int32_t)nchunk);
-    const TeamLayout L = team_layout(nnear, nchunk, clen, csz, (uint32_t)vsz);
+    const TeamLayout L = team_layout(nnear, slot_major ? nmax : 0, nchunk, clen, csz, (uint32_t)vsz);
     const size_t base = P.bytes.size();
     P.bytes.resize(base + L.len, 0);
     unsigned char *p = P.bytes.data() + base;
@@ -285,10 +295,10 @@ void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
     noff[0] = 0;
     size_t w = 0;
     for (int r = 0; r < BS; ++r) {
-      for (auto &en : nearl[r]) {
-        p[L.o_ncol + w] = (unsigned char)en.first;
-        put_val(L.o_nval, w, en.second);
-        ++w;
+      for (size_t j = 0; j < nearl[r].size(); ++j, ++w) {
+        const size_t at = slot_major ? j * BS + r : w;
+        p[L.o_ncol + at] = (unsigned char)nearl[r][j].first;
+        put_val(L.o_nval, at, nearl[r][j].second);
       }
       noff[r + 1] = (uint16_t)w;
       for (size_t q = 0; q < farl[r].size(); ++q) {  // entry q of row r: chunk crow[r] + q / clen, slot q % clen
@@ -302,7 +312,7 @@ void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
         put_val(L.o_fval, at, farl[r][q].second);
       }
     }
-    std::memcpy(p + L.o_noff, noff, sizeof(noff));
+    if (!slot_major) std::memcpy(p + L.o_noff, noff, sizeof(noff));
     std::memcpy(p + L.o_crow, crow, sizeof(crow));
     for (int c = 0; c < BS; ++c) {
       const int r_lo = upper ? 0 : c, r_hi = upper ? c : BS - 1;
@@ -602,7 +612,7 @@ __device__ __forceinline__ void helpers_sync(int nthreads) {
 // The solver's chain per step is therefore only shuffles and FMAs; every
 // load it issues is independent of the previous block.
 template <typename VT, typename OutT, bool UPPER>
-__global__ void __launch_bounds__(256, 2) team_kernel(TeamArgs<VT> a, OutT *out) {
+__global__ void __launch_bounds__(512, 1) team_kernel(TeamArgs<VT> a, OutT *out) {
   extern __shared__ __align__(16) unsigned char smem[];
   const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -786,21 +796,22 @@ __global__ void __launch_bounds__(256, 1) team_k_kernel(TeamArgs<VT> a, OutT *ou
       const unsigned char *p = ring + (size_t)(b % RING) * a.bufbytes;
       const TeamHdr h = read_hdr(p);
       const uint32_t nr = h.nr, row0 = h.row0, prow0 = h.prow0;
-      const uint16_t *noff = reinterpret_cast<const uint16_t *>(p + h.o_noff);
       const unsigned char *ncol = p + h.o_ncol;
       const VT *nval = reinterpret_cast<const VT *>(p + h.o_nval);
       const VT *minv = reinterpret_cast<const VT *>(p + h.o_min);
       const VT *pb = part + (size_t)(b & 1) * BS * KW;
       VT t[BS];
 #pragma unroll
-      for (int r = 0; r < BS; ++r) {
-        VT s = 0;
-        if (r < (int)nr) {
-          s = xs[(row0 + r) * KW + lane] - pb[r * KW + lane];
-          for (uint32_t e = noff[r]; e < noff[r + 1]; ++e) s -= nval[e] * xs[(prow0 + ncol[e]) * KW + lane];
-        }
-        t[r] = s;
+      for (int r = 0; r < BS; ++r) t[r] = r < (int)nr ? xs[(row0 + r) * KW + lane] - pb[r * KW + lane] : VT(0);
+      // near entries, slot by slot: the 32 rows of a slot are independent
+      for (uint32_t j = 0; j < h.nmax; ++j) {
+#pragma unroll
+        for (int r = 0; r < BS; ++r)
+          t[r] -= nval[j * BS + r] * xs[(prow0 + ncol[j * BS + r]) * KW + lane];
       }
+#pragma unroll
+      for (int r = 0; r < BS; ++r)
+        if (r >= (int)nr) t[r] = VT(0);
       // x = T^-1 t in place: lower rows from the last up, upper from the first down
 #pragma unroll
       for (int i = 0; i < BS; ++i) {
@@ -860,6 +871,21 @@ __global__ void __launch_bounds__(256, 1) team_k_kernel(TeamArgs<VT> a, OutT *ou
 
 // ---- plan construction ---------------------------------------------------------------
 
+// SM count of the current device (a scheduling heuristic only: without a
+// device, as in host-side plan checks, the GB300's 152 is assumed).
+static int sm_count() {
+  static int count = 0;
+  if (!count) {
+    int dev = 0, c = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && c > 0)
+      count = c;
+    else
+      count = 152;
+  }
+  return count;
+}
+
 // Host copy of one direction's stream (development checks decode it on the CPU).
 struct HostStreamCopy {
   std::vector<unsigned char> blocks;
@@ -886,9 +912,17 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   // record counts every entry of its rows that lies in the node but outside
   // the block (an upper bound of its sparse part).
   const size_t budget = 200 * 1024;
-  const int helper_threads = 32 * (D.team_warps - 1);
   int maxdepth = 1;
   for (auto &nd : tnodes) maxdepth = std::max(maxdepth, nd.depth);
+  // Team size per depth: where few pieces share the GPU (one per SM or fewer
+  // in flight) the team doubles, halving every helper's share of the far
+  // entries; elsewhere residency matters more.
+  std::vector<int> depth_nodes(maxdepth + 1, 0);
+  for (auto &nd : tnodes)
+    if (std::min(nd.end, n) > nd.begin) ++depth_nodes[nd.depth];
+  auto team_warps_of = [&](int depth) {
+    return kwidth == 1 && D.team_warps == 8 && depth_nodes[depth] <= 2 * sm_count() ? 16 : D.team_warps;
+  };
   // team format for separators (few, long chains), warp format for leaves
   auto team_depth = [&](int depth) {
     if (team_mode == 0) return false;
@@ -897,8 +931,10 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   struct Piece {
     int64_t b, e;
     bool team;
+    int warps;
   };
-  auto cut_node = [&](int64_t b, int64_t e, bool team) {
+  auto cut_node = [&](int64_t b, int64_t e, bool team, int warps) {
+    const int helper_threads = 32 * (warps - 1);
     std::vector<Piece> out;
     const int64_t nb = (e - b + BS - 1) / BS;
     std::vector<size_t> recb(nb);
@@ -929,7 +965,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
       }
       if (fixed + nrec * al16(mx) + (size_t)(std::min(e, b + k1 * BS) - (b + k * BS)) * row_bytes > budget)
         throw Error(RCHOL_ERR_INTERNAL, "a 32-row block of G is too dense for the shared-memory solve");
-      out.push_back(Piece{b + k * BS, std::min(e, b + k1 * BS), team});
+      out.push_back(Piece{b + k * BS, std::min(e, b + k1 * BS), team, warps});
       k = k1;
     }
     return out;
@@ -948,7 +984,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
       std::vector<Piece> ps;
       bool team = team_depth(depth) && !team_failed[depth];
       try {
-        ps = cut_node(b, e, team);
+        ps = cut_node(b, e, team, team_warps_of(depth));
       } catch (const Error &) {
         if (!team || kwidth > 1) throw;
         // a block too dense for the team ring: this depth uses the warp format
@@ -1005,7 +1041,8 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   parallel_for(np, [&](int64_t k0, int64_t k1) {
     for (int64_t k = k0; k < k1; ++k) {
       if (pieces[k].team)
-        build_team_piece(rp, ci, v, pieces[k].b, pieces[k].e, upper, vsz, helper_threads, built[k], chunks[k]);
+        build_team_piece(rp, ci, v, pieces[k].b, pieces[k].e, upper, vsz, 32 * (pieces[k].warps - 1), kwidth > 1,
+                         built[k], chunks[k]);
       else
         build_piece(rp, ci, v, pieces[k].b, pieces[k].e, upper, vsz, built[k]);
     }
@@ -1037,6 +1074,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   D.stage_rows.clear();
   D.stage_maxrec.clear();
   D.stage_team.clear();
+  D.stage_warps.clear();
   D.stage_chunks.clear();
   D.stage_ext_lanes.clear();
   D.stage_row_ptr.assign(1, 0);
@@ -1059,6 +1097,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     D.stage_rows.push_back(rows);
     D.stage_maxrec.push_back(maxrec);
     D.stage_team.push_back(team ? 1 : 0);
+    D.stage_warps.push_back(D.stage_ptr[st + 1] > D.stage_ptr[st] ? pieces[D.stage_ptr[st]].warps : D.team_warps);
     D.stage_chunks.push_back(std::max(1, maxchunk));
     D.stage_ext_lanes.push_back(avg < 6 ? 1 : avg < 24 ? 4 : avg < 96 ? 8 : 32);
     D.stage_row_ptr.push_back((int64_t)srows.size());
@@ -1140,16 +1179,6 @@ void build_streams_k(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
 
 // ---- launch ------------------------------------------------------------------------------
 
-static int sm_count() {
-  static int count = 0;
-  if (!count) {
-    int dev = 0, c = 0;
-    RCHOL_CUDA(cudaGetDevice(&dev));
-    RCHOL_CUDA(cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev));
-    count = std::max(1, c);
-  }
-  return count;
-}
 
 template <typename VT, typename InT, typename OutT>
 static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *out, VT *acc, cudaStream_t s) {
@@ -1218,7 +1247,7 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       ta.ring = ring;
       const size_t bytes = (size_t)ring * ta.bufbytes + fixed;
       if (bytes > (size_t)smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
-      const unsigned threads = 32u * (unsigned)D.team_warps;
+      const unsigned threads = 32u * (unsigned)D.stage_warps[st];
       if (upper) team_kernel<VT, OutT, true><<<pieces, threads, bytes, s>>>(ta, out);
       else team_kernel<VT, OutT, false><<<pieces, threads, bytes, s>>>(ta, out);
     } else {
