@@ -60,6 +60,14 @@ int64_t rchol_gpu_launch_count(void);
  * entries, the last one counting the ground vertex). */
 int rchol_gpu_tree_build(int64_t n, const int64_t *row_ptr, const int64_t *col_idx,
                          int threads, rchol_tree_t *out);
+/* The same with ordering flags.  RCHOL_ORDER_LAST_IN_ROOT reproduces the
+ * Python front end's ordering, which forces the last vertex into the root
+ * separator (python/rchol_lap/find_separator.pyx:27-28, called from
+ * python/rchol/rchol.py:31-33); without it the ordering is the C++ front
+ * end's (c++/rchol/find_separator.cpp). */
+#define RCHOL_ORDER_LAST_IN_ROOT 1
+int rchol_gpu_tree_build_ex(int64_t n, const int64_t *row_ptr, const int64_t *col_idx,
+                            int threads, int flags, rchol_tree_t *out);
 /* Many independent systems at once (no counterpart in the reference, which
  * orders one matrix per call): the matrix is block diagonal with system s on
  * rows [sys_ptr[s], sys_ptr[s+1]).  Each system is ordered like

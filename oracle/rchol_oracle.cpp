@@ -426,8 +426,10 @@ Csr submatrix(const std::vector<uint64_t> &par, const std::vector<int64_t> &sep,
   return B;
 }
 
+// last_in_root: python/rchol_lap/find_separator.pyx:27-28 (the Python front
+// end forces the last vertex into the root separator).
 void find_sep(const Csr &A, int depth, int target, std::vector<uint64_t> &p,
-              std::vector<uint64_t> &val) {
+              std::vector<uint64_t> &val, bool last_in_root = false) {
   if (depth == target) {
     val.assign(1, (uint64_t)A.n);
     p.resize(A.n);
@@ -436,6 +438,7 @@ void find_sep(const Csr &A, int depth, int target, std::vector<uint64_t> &p,
   }
   if (A.n <= 1) throw std::invalid_argument("too many threads requested");
   std::vector<int64_t> sep = metis_sep(A);
+  if (last_in_root && depth == 1) sep[A.n - 1] = 2;
   std::vector<uint64_t> l, r, s;
   for (int64_t i = 0; i < A.n; ++i) {
     if (sep[i] == 0) l.push_back(i);
@@ -652,8 +655,8 @@ int oracle_reorder(int64_t n, const uint64_t *rp, const uint64_t *ci, const doub
 
 // c++/rchol/rchol_parallel.cpp:37-70: remove the diagonal, nested dissection
 // to depth log2(threads)+1, result_idx with the ground vertex in the root.
-int oracle_order(int64_t n, const uint64_t *rp, const uint64_t *ci, int threads,
-                 uint64_t **perm, uint64_t **ridx, int64_t *nridx) {
+int oracle_order_ex(int64_t n, const uint64_t *rp, const uint64_t *ci, int threads, int last_in_root,
+                    uint64_t **perm, uint64_t **ridx, int64_t *nridx) {
   try {
     if (threads <= 0) throw std::invalid_argument("thread number should be positive");
     if ((threads & (threads - 1)) != 0)
@@ -669,7 +672,7 @@ int oracle_order(int64_t n, const uint64_t *rp, const uint64_t *ci, int threads,
     int target = 1;
     while ((1 << (target - 1)) < threads) ++target;
     std::vector<uint64_t> p, val;
-    find_sep(A, 1, target, p, val);
+    find_sep(A, 1, target, p, val, last_in_root != 0);
     std::vector<uint64_t> ri{0};
     for (uint64_t x : val) ri.push_back(ri.back() + x);
     ri.back() += 1;
@@ -681,6 +684,11 @@ int oracle_order(int64_t n, const uint64_t *rp, const uint64_t *ci, int threads,
     g_err = e.what();
     return 1;
   }
+}
+
+int oracle_order(int64_t n, const uint64_t *rp, const uint64_t *ci, int threads,
+                 uint64_t **perm, uint64_t **ridx, int64_t *nridx) {
+  return oracle_order_ex(n, rp, ci, threads, 0, perm, ridx, nridx);
 }
 
 // Factor the extended Laplacian L (upper CSR, positive edge weights, as

@@ -48,15 +48,20 @@ def _csr(A):
     return A
 
 
-def rchol(A, nt=1, perm=np.array([]), part=np.array([]), seed=0, precision="fp64"):
+def rchol(A, nt=1, perm=np.array([]), part=np.array([]), seed=0, precision="fp64", order="python"):
     """Randomized Cholesky preconditioner of an SDDM matrix on the GPU.
 
     Mirrors python/rchol/rchol.py:8-45.  ``nt`` is the number of leaf
     subdomains of the nested-dissection tree (the reference's thread count,
     a power of two); ``perm``/``part`` reuse an earlier ordering and must be
-    given together.  Returns ``(G, perm, part)`` with G lower triangular such
-    that G G^T approximates A[perm][:, perm].
+    given together.  ``order="python"`` is the Python front end's nested
+    dissection (the last vertex goes into the root separator,
+    python/rchol_lap/find_separator.pyx:27-28), ``"c++"`` the C++ front
+    end's.  Returns ``(G, perm, part)`` with G lower triangular such that
+    G G^T approximates A[perm][:, perm].
     """
+    if order not in ("python", "c++"):
+        raise ValueError("order must be 'python' or 'c++'")
     if nt < 1:
         raise Exception("number of threads must be at least 1")
     perm = np.asarray(perm)
@@ -68,7 +73,7 @@ def rchol(A, nt=1, perm=np.array([]), part=np.array([]), seed=0, precision="fp64
         print("number of threads rounded down to {}".format(nt))
     A = _csr(A)
     if perm.size == 0:
-        tree = Tree.build(A.indptr, A.indices, nt)
+        tree = Tree.build(A.indptr, A.indices, nt, last_in_root=(order == "python"))
     else:
         tree = Tree.from_partition(perm, part)
     perm, part = tree.arrays()

@@ -29,6 +29,7 @@ SIGNATURES = [
     ("rchol_gpu_version", C.c_char_p, []),
     ("rchol_gpu_launch_count", _i64, []),
     ("rchol_gpu_tree_build", C.c_int, [_i64, _i64p, _i64p, C.c_int, C.POINTER(_vp)]),
+    ("rchol_gpu_tree_build_ex", C.c_int, [_i64, _i64p, _i64p, C.c_int, C.c_int, C.POINTER(_vp)]),
     ("rchol_gpu_tree_build_batch", C.c_int, [_i64, _i64p, _i64, _i64p, _i64p, C.c_int, C.POINTER(_vp)]),
     ("rchol_gpu_tree_from_partition", C.c_int, [_i64, _i64p, _i64p, _i64, C.POINTER(_vp)]),
     ("rchol_gpu_tree_size", _i64, [_vp]),
@@ -134,10 +135,13 @@ class Tree(Handle):
     _destroy = "rchol_gpu_tree_destroy"
 
     @classmethod
-    def build(cls, rowptr, colidx, threads):
+    def build(cls, rowptr, colidx, threads, last_in_root=False):
+        """Nested dissection with ``threads`` leaves; ``last_in_root`` gives the
+        Python front end's variant (last vertex in the root separator)."""
         rp, ci = i64(rowptr), i64(colidx)
         out = _vp()
-        check(lib().rchol_gpu_tree_build(len(rp) - 1, p64(rp), p64(ci), int(threads), C.byref(out)))
+        check(lib().rchol_gpu_tree_build_ex(len(rp) - 1, p64(rp), p64(ci), int(threads), 1 if last_in_root else 0,
+                                            C.byref(out)))
         return cls(out)
 
     @classmethod

@@ -78,6 +78,16 @@ int rchol_gpu_tree_build(int64_t n, const int64_t *row_ptr, const int64_t *col_i
   API_END
 }
 
+int rchol_gpu_tree_build_ex(int64_t n, const int64_t *row_ptr, const int64_t *col_idx, int threads, int flags,
+                            rchol_tree_t *out) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(out, "null output handle");
+  RCHOL_CHECK_ARG((flags & ~RCHOL_ORDER_LAST_IN_ROOT) == 0, "unknown ordering flags");
+  *out = nullptr;
+  *out = build_tree(n, row_ptr, col_idx, threads, (flags & RCHOL_ORDER_LAST_IN_ROOT) != 0);
+  API_END
+}
+
 int rchol_gpu_tree_build_batch(int64_t nsys, const int64_t *sys_ptr, int64_t n, const int64_t *row_ptr,
                                const int64_t *col_idx, int threads, rchol_tree_t *out) {
   API_BEGIN

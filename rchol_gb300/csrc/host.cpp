@@ -101,7 +101,7 @@ int64_t segments(int levels) { return ((int64_t)1 << levels) - 1; }
 // mapping and exits without touching anything else.  Each METIS call sees
 // exactly the subgraph the serial recursion would give it, so the ordering is
 // identical to the serial one.
-void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks);
+void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks, bool last_in_root = false);
 
 bool dissect_in_child(Graph &g, int depth, int target, int64_t *p, int64_t *val, int forks,
                       pid_t *pid_out, int64_t **shm_out, size_t *shm_bytes) {
@@ -150,7 +150,9 @@ void collect_child(pid_t pid, int64_t *shm, size_t bytes, int64_t n, int64_t nse
   if (status != 0) throw Error(RCHOL_ERR_INTERNAL, "nested-dissection worker process failed");
 }
 
-void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks) {
+// last_in_root: the Python front end's variant, which puts the last vertex
+// into the root separator (python/rchol_lap/find_separator.pyx:27-28).
+void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks, bool last_in_root) {
   if (depth == target) {
     val[0] = g.n;
     for (int64_t i = 0; i < g.n; ++i) p[i] = i;
@@ -158,6 +160,7 @@ void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks
   }
   if (g.n <= 1) throw Error(RCHOL_ERR_INVALID, "too many threads requested");
   std::vector<int64_t> label = metis_separator(g);
+  if (last_in_root && depth == 1) label[g.n - 1] = 2;
   std::vector<int64_t> l, r, s;
   for (int64_t i = 0; i < g.n; ++i) {
     if (label[i] == 0) l.push_back(i);
@@ -237,7 +240,7 @@ void validate_csr(int64_t n, const int64_t *rp, const int64_t *ci) {
   }
 }
 
-rchol_tree_s *build_tree(int64_t n, const int64_t *rp, const int64_t *ci, int threads) {
+rchol_tree_s *build_tree(int64_t n, const int64_t *rp, const int64_t *ci, int threads, bool last_in_root) {
   RCHOL_CHECK_ARG(threads > 0, "thread number should be positive");
   RCHOL_CHECK_ARG((threads & (threads - 1)) == 0, "thread number should be a power of 2");
   validate_csr(n, rp, ci);
@@ -275,7 +278,7 @@ rchol_tree_s *build_tree(int64_t n, const int64_t *rp, const int64_t *ci, int th
       if (const char *e = getenv("RCHOL_ORDER_FORK_LEVELS")) forks = atoi(e);
       t->perm.resize(n);
       val.resize(segments(target));
-      dissect(std::move(g), 1, target, t->perm.data(), val.data(), forks);
+      dissect(std::move(g), 1, target, t->perm.data(), val.data(), forks, last_in_root);
     }
     t->part.assign(1, 0);
     for (int64_t x : val) t->part.push_back(t->part.back() + x);

@@ -612,7 +612,7 @@ __device__ __forceinline__ void helpers_sync(int nthreads) {
 // The solver's chain per step is therefore only shuffles and FMAs; every
 // load it issues is independent of the previous block.
 template <typename VT, typename OutT, bool UPPER>
-__global__ void __launch_bounds__(512, 1) team_kernel(TeamArgs<VT> a, OutT *out) {
+__global__ void __launch_bounds__(256, 2) team_kernel(TeamArgs<VT> a, OutT *out) {
   extern __shared__ __align__(16) unsigned char smem[];
   const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -914,15 +914,10 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   const size_t budget = 200 * 1024;
   int maxdepth = 1;
   for (auto &nd : tnodes) maxdepth = std::max(maxdepth, nd.depth);
-  // Team size per depth: where few pieces share the GPU (one per SM or fewer
-  // in flight) the team doubles, halving every helper's share of the far
-  // entries; elsewhere residency matters more.
-  std::vector<int> depth_nodes(maxdepth + 1, 0);
-  for (auto &nd : tnodes)
-    if (std::min(nd.end, n) > nd.begin) ++depth_nodes[nd.depth];
-  auto team_warps_of = [&](int depth) {
-    return kwidth == 1 && D.team_warps == 8 && depth_nodes[depth] <= 2 * sm_count() ? 16 : D.team_warps;
-  };
+  // One team size for all depths: doubling the team where few pieces run
+  // measured slower (the extra helpers' barrier and shared-memory traffic
+  // cost more than their shorter chunks save).
+  auto team_warps_of = [&](int) { return D.team_warps; };
   // team format for separators (few, long chains), warp format for leaves
   auto team_depth = [&](int depth) {
     if (team_mode == 0) return false;

@@ -19,6 +19,40 @@ def test_ordering_bit_exact(O, R, n, threads):
     assert part[-1] == A.shape[0] + 1 and len(part) == 2 * threads
 
 
+@pytest.mark.parametrize("n,threads", [(8, 2), (12, 8), (16, 32)])
+def test_ordering_python_front_end_variant(O, R, n, threads):
+    """The Python front end's ordering (last vertex forced into the root
+    separator, python/rchol_lap/find_separator.pyx:27-28), bit-exact."""
+    A = R.laplace_3d(n)
+    tree = R.Tree.build(A.indptr, A.indices, threads, last_in_root=True)
+    perm, part = tree.arrays()
+    po, ro = O.order(csr_u64(A), threads, last_in_root=True)
+    assert np.array_equal(perm, po.astype(np.int64))
+    assert np.array_equal(part, ro.astype(np.int64))
+    root = perm[part[-2]:part[-1] - 1]  # the root separator (ground excluded)
+    assert A.shape[0] - 1 in root
+    plain, _ = R.Tree.build(A.indptr, A.indices, threads).arrays()
+    assert not np.array_equal(plain, perm) or A.shape[0] - 1 in plain[part[-2]:]
+
+
+def test_ordering_python_variant_matches_reference_fixture(O, R):
+    """Against the reference's own Cython find_separator, run as
+    python/rchol/rchol.py does (tests/golden/make_python_order.py)."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "python_order.npz"))
+    cases = sorted({k.split("_", 1)[1] for k in g.files})
+    assert cases
+    for case in cases:
+        n, nt = (int(x) for x in case.split("_"))
+        A = R.laplace_3d(n)
+        perm, part = R.Tree.build(A.indptr, A.indices, nt, last_in_root=True).arrays()
+        assert np.array_equal(perm, g["perm_" + case]), case
+        assert np.array_equal(part, g["part_" + case]), case
+        po, ro = O.order(csr_u64(A), nt, last_in_root=True)
+        assert np.array_equal(po.astype(np.int64), g["perm_" + case]), case
+
+
 def test_ordering_forked_workers_match_serial(O, R, monkeypatch):
     """Large enough that subtrees go to forked worker processes."""
     A = R.laplace_3d(40)
