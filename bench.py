@@ -66,6 +66,17 @@ def dist_init(args):
     return rank, local, world, pg
 
 
+def max_over_ranks(value, pg, device):
+    """The slowest replica's time: every rank gets max(value) over ranks."""
+    if pg is None:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
 
@@ -208,11 +219,7 @@ def run_gb300(args, rank, local, world, pg):
             out = fn()
         e1.record(stream)
         barrier()
-        ms = e0.elapsed_time(e1) / steps
-        if pg is not None:
-            t = torch.tensor([ms], device=dev)
-            pg.all_reduce(t, op=pg.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps, pg, dev)
         return ms, out
 
     launches0 = L.rchol_gpu_launch_count()
@@ -264,11 +271,7 @@ def run_gb300(args, rank, local, world, pg):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         solve_host()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    if pg is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, pg, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
