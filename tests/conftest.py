@@ -9,7 +9,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
+# reference path fixtures (tests/golden/make_golden.py); python_order.npz is
+# the ordering-only fixture of tests/golden/make_python_order.py
+GOLDEN = sorted(p for p in glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz"))
+                if not os.path.basename(p).startswith("python_order"))
 
 
 def pytest_configure(config):
