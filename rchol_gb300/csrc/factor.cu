@@ -107,6 +107,52 @@ __device__ __forceinline__ bool wless(double wa, uint32_t ra, double wb, uint32_
   return wa < wb || (wa == wb && ra < rb);
 }
 
+// In-place ascending sort of n records (key[i], val[i]) by one warp: a
+// bitonic network whose merges compare each element with its mirror, so
+// every comparator points the same way and the missing elements past n
+// behave as +infinity (comparators reaching past n are skipped).  O(n log^2 n)
+// work against the O(n^2) of a rank sort; used for wide columns.  The keys of
+// a column are unique, so the order equals any other sort's.
+template <typename K, typename V, typename Less>
+__device__ void warp_bitonic_sort(K *key, V *val, int n, Less less) {
+  const int lane = threadIdx.x & 31;
+  int npow = 1;
+  while (npow < n) npow <<= 1;
+  const int half = npow >> 1;
+  for (int k = 2; k <= npow; k <<= 1) {
+    const int hk = k >> 1;
+    for (int t = lane; t < half; t += 32) {  // mirror stage
+      const int blk = t / hk, o = t - blk * hk;
+      const int i = blk * k + o, j = blk * k + k - 1 - o;
+      if (j < n && less(key[j], val[j], key[i], val[i])) {
+        const K tk = key[i];
+        key[i] = key[j];
+        key[j] = tk;
+        const V tv = val[i];
+        val[i] = val[j];
+        val[j] = tv;
+      }
+    }
+    __syncwarp();
+    for (int d = hk >> 1; d >= 1; d >>= 1) {  // half cleaners
+      for (int t = lane; t < half; t += 32) {
+        const int i = (t / d) * 2 * d + (t % d), j = i + d;
+        if (j < n && less(key[j], val[j], key[i], val[i])) {
+          const K tk = key[i];
+          key[i] = key[j];
+          key[j] = tk;
+          const V tv = val[i];
+          val[i] = val[j];
+          val[j] = tv;
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+constexpr int RANK_SORT_MAX = 64;  // wider columns use the bitonic network
+
 __global__ void eliminate_kernel(ElimArgs a) {
   extern __shared__ unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
@@ -166,12 +212,21 @@ __global__ void eliminate_kernel(ElimArgs a) {
     }
     __syncwarp();
     // ---- 2. sort by (row, source) and merge --------------------------------
-    for (int e = lane; e < total; e += 32) {
-      uint64_t ke = akey[e];
-      int rank = 0;
-      for (int f = 0; f < total; ++f) rank += (akey[f] < ke);
-      bkey[rank] = ke;
-      bval[rank] = aval[e];
+    if (total <= RANK_SORT_MAX) {
+      for (int e = lane; e < total; e += 32) {
+        uint64_t ke = akey[e];
+        int rank = 0;
+        for (int f = 0; f < total; ++f) rank += (akey[f] < ke);
+        bkey[rank] = ke;
+        bval[rank] = aval[e];
+      }
+    } else {
+      warp_bitonic_sort(akey, aval, total,
+                        [](uint64_t ka, double, uint64_t kb, double) { return ka < kb; });
+      for (int e = lane; e < total; e += 32) {
+        bkey[e] = akey[e];
+        bval[e] = aval[e];
+      }
     }
     __syncwarp();
     int m = 0;
@@ -195,13 +250,25 @@ __global__ void eliminate_kernel(ElimArgs a) {
     }
     __syncwarp();
     // ---- 3. sort by (weight, row), prefix sum --------------------------------
-    for (int e = lane; e < m; e += 32) {
-      double we = aval[e];
-      uint32_t re = (uint32_t)akey[e];
-      int rank = 0;
-      for (int f = 0; f < m; ++f) rank += wless(aval[f], (uint32_t)akey[f], we, re);
-      bkey[rank] = re;
-      bval[rank] = we;
+    if (m <= RANK_SORT_MAX) {
+      for (int e = lane; e < m; e += 32) {
+        double we = aval[e];
+        uint32_t re = (uint32_t)akey[e];
+        int rank = 0;
+        for (int f = 0; f < m; ++f) rank += wless(aval[f], (uint32_t)akey[f], we, re);
+        bkey[rank] = re;
+        bval[rank] = we;
+      }
+    } else {
+      for (int e = lane; e < m; e += 32) {
+        bkey[e] = (uint32_t)akey[e];
+        bval[e] = aval[e];
+      }
+      __syncwarp();
+      warp_bitonic_sort(bkey, bval, m,
+                        [](uint64_t ra, double wa, uint64_t rb, double wb) {
+                          return wless(wa, (uint32_t)ra, wb, (uint32_t)rb);
+                        });
     }
     __syncwarp();
     double carry = 0.0;

@@ -557,7 +557,7 @@ struct TeamArgs {
   const VT *acc;
 };
 
-constexpr int TEAM_RING = 4;  // smallest ring, used to cut pieces; launches deepen it where room is left
+constexpr int TEAM_RING = 4;  // ring used to cut pieces; launches deepen it where room is left (3 at least)
 constexpr int TEAM_RING_MAX = 8;
 
 // cp.async.wait_group takes an immediate: wait until at most n groups pend.
@@ -958,7 +958,10 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
         mx = m2;
         ++k1;
       }
-      if (fixed + nrec * al16(mx) + (size_t)(std::min(e, b + k1 * BS) - (b + k * BS)) * row_bytes > budget)
+      // a single block may run with the smallest ring (3 records: no copy in
+      // flight across a step) rather than fall back to the warp format
+      const size_t nmin = team ? 3 : 2;
+      if (fixed + nmin * al16(mx) + (size_t)(std::min(e, b + k1 * BS) - (b + k * BS)) * row_bytes > budget)
         throw Error(RCHOL_ERR_INTERNAL, "a 32-row block of G is too dense for the shared-memory solve");
       out.push_back(Piece{b + k * BS, std::min(e, b + k1 * BS), team, warps});
       k = k1;
@@ -1238,7 +1241,7 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       // where few pieces share the GPU; where many do, they hide each
       // other's latency and shared memory goes to residency instead
       int ring = pieces > 2 * sm_count() ? 5 : TEAM_RING_MAX;
-      while (ring > TEAM_RING && fixed + (size_t)ring * ta.bufbytes > (size_t)smem_cap) --ring;
+      while (ring > 3 && fixed + (size_t)ring * ta.bufbytes > (size_t)smem_cap) --ring;
       ta.ring = ring;
       const size_t bytes = (size_t)ring * ta.bufbytes + fixed;
       if (bytes > (size_t)smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
@@ -1317,7 +1320,7 @@ static void launch_streams_k(const SolvePlan &P, bool upper, const InT *in, OutT
     ta.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
     const size_t fixed = 2 * (size_t)BS * KW * sizeof(VT) + (size_t)D.stage_rows[st] * KW * sizeof(VT);
     int ring = pieces > 2 * sm_count() ? 5 : TEAM_RING_MAX;
-    while (ring > TEAM_RING && fixed + (size_t)ring * ta.bufbytes > (size_t)smem_cap) --ring;
+    while (ring > 3 && fixed + (size_t)ring * ta.bufbytes > (size_t)smem_cap) --ring;
     ta.ring = ring;
     const size_t bytes = (size_t)ring * ta.bufbytes + fixed;
     if (bytes > (size_t)smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
