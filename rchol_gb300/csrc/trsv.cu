@@ -301,15 +301,66 @@ void build_team_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
         put_val(L.o_nval, at, nearl[r][j].second);
       }
       noff[r + 1] = (uint16_t)w;
-      for (size_t q = 0; q < farl[r].size(); ++q) {  // entry q of row r: chunk crow[r] + q / clen, slot q % clen
-        const size_t at = (size_t)(q % clen) * nchunk + crow[r] + q / clen;
-        if (csz == 2) {
-          const uint16_t c16 = (uint16_t)farl[r][q].first;
-          std::memcpy(p + L.o_fcol + 2 * at, &c16, 2);
-        } else {
-          std::memcpy(p + L.o_fcol + 4 * at, &farl[r][q].first, 4);
+    }
+    // Far entries of chunk c (row r's entries crow[r]*clen.. in column order,
+    // clen per chunk), then placed slot by slot.  Helper thread c sums chunk
+    // c, so in step j the 32 lanes of a helper warp gather the solved values
+    // of slot j of 32 consecutive chunks: within a warp's chunks the entries
+    // of each step are chosen greedily so that those gathers hit distinct
+    // shared-memory banks where possible (the sum of a chunk does not depend
+    // on that order beyond rounding); padding entries (value 0) take a
+    // column of a bank that is still free.
+    std::vector<std::vector<std::pair<uint32_t, double>>> chunkl(nchunk);
+    for (int r = 0; r < BS; ++r)
+      for (size_t q = 0; q < farl[r].size(); ++q) chunkl[crow[r] + q / clen].push_back(farl[r][q]);
+    const uint32_t nbank = vsz == 4 ? 32 : 16;  // words of one entry of the unknowns
+    const int64_t piece_rows = e - b;
+    for (uint32_t g0 = 0; g0 < nchunk; g0 += 32) {
+      const uint32_t g1 = std::min(nchunk, g0 + 32);
+      std::vector<std::vector<char>> taken(g1 - g0);
+      for (uint32_t c = g0; c < g1; ++c) taken[c - g0].assign(chunkl[c].size(), 0);
+      for (uint32_t j = 0; j < clen; ++j) {
+        std::vector<char> busy(nbank, 0);
+        std::vector<int> pick(g1 - g0, -1);
+        for (uint32_t c = g0; c < g1; ++c) {  // a free bank first, else the first remaining entry
+          const auto &lst = chunkl[c];
+          int first = -1;
+          for (size_t q = 0; q < lst.size(); ++q) {
+            if (taken[c - g0][q]) continue;
+            if (first < 0) first = (int)q;
+            if (!busy[lst[q].first % nbank]) {
+              pick[c - g0] = (int)q;
+              break;
+            }
+          }
+          if (pick[c - g0] < 0) pick[c - g0] = first;
+          if (pick[c - g0] >= 0) {
+            taken[c - g0][pick[c - g0]] = 1;
+            busy[lst[pick[c - g0]].first % nbank] = 1;
+          }
         }
-        put_val(L.o_fval, at, farl[r][q].second);
+        for (uint32_t c = g0; c < g1; ++c) {
+          uint32_t col;
+          double val;
+          if (pick[c - g0] >= 0) {
+            col = chunkl[c][pick[c - g0]].first;
+            val = chunkl[c][pick[c - g0]].second;
+          } else {  // padding
+            uint32_t bank = 0;
+            while (bank + 1 < nbank && (busy[bank] || bank >= piece_rows)) ++bank;
+            busy[bank] = 1;
+            col = bank < piece_rows ? bank : 0;
+            val = 0.0;
+          }
+          const size_t at = (size_t)j * nchunk + c;
+          if (csz == 2) {
+            const uint16_t c16 = (uint16_t)col;
+            std::memcpy(p + L.o_fcol + 2 * at, &c16, 2);
+          } else {
+            std::memcpy(p + L.o_fcol + 4 * at, &col, 4);
+          }
+          put_val(L.o_fval, at, val);
+        }
       }
     }
     if (!slot_major) std::memcpy(p + L.o_noff, noff, sizeof(noff));
