@@ -66,6 +66,11 @@ int rchol_gpu_tree_build(int64_t n, const int64_t *row_ptr, const int64_t *col_i
  * python/rchol/rchol.py:31-33); without it the ordering is the C++ front
  * end's (c++/rchol/find_separator.cpp). */
 #define RCHOL_ORDER_LAST_IN_ROOT 1
+/* Fill-reducing order inside every leaf subdomain instead of the natural one
+ * (the MATLAB front end orders leaves with amd, matlab/rchol/find_separator.m:6):
+ * METIS nested dissection, or a minimum-degree ordering (for small leaves). */
+#define RCHOL_ORDER_LEAF_ND 2
+#define RCHOL_ORDER_LEAF_MD 4
 int rchol_gpu_tree_build_ex(int64_t n, const int64_t *row_ptr, const int64_t *col_idx,
                             int threads, int flags, rchol_tree_t *out);
 /* Many independent systems at once (no counterpart in the reference, which

@@ -107,14 +107,16 @@ class Oracle(_Lib):
                                 _p(_u64(perm), _u64p), C.byref(orp), C.byref(oci), C.byref(ov))
         return self.take_csr(orp, oci, ov, n)
 
-    def order(self, A, threads, last_in_root=False):
+    def order(self, A, threads, last_in_root=False, leaf_order="natural"):
         """Nested-dissection ordering; last_in_root: the Python front end's
-        variant (python/rchol_lap/find_separator.pyx:27-28)."""
+        variant (python/rchol_lap/find_separator.pyx:27-28); leaf_order:
+        "natural", "nd" or "md" inside the leaves."""
         rp, ci = A[0], A[1]
         n = len(rp) - 1
         perm, ridx, nr = _u64p(), _u64p(), _i64()
         rc = self.lib.oracle_order_ex(_i64(n), _p(_u64(rp), _u64p), _p(_u64(ci), _u64p), int(threads),
-                                      int(bool(last_in_root)), C.byref(perm), C.byref(ridx), C.byref(nr))
+                                      int(bool(last_in_root)) | {"natural": 0, "nd": 2, "md": 4}[leaf_order],
+                                      C.byref(perm), C.byref(ridx), C.byref(nr))
         if rc:
             raise ValueError(self.err())
         return self.take(perm, n, np.uint64), self.take(ridx, nr.value, np.uint64)

@@ -32,6 +32,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <set>
 #include <random>
 #include <stdexcept>
 #include <string>
@@ -428,12 +429,50 @@ Csr submatrix(const std::vector<uint64_t> &par, const std::vector<int64_t> &sep,
 
 // last_in_root: python/rchol_lap/find_separator.pyx:27-28 (the Python front
 // end forces the last vertex into the root separator).
+// Leaf order (no counterpart in the C++ reference, which keeps the natural
+// order; the MATLAB front end uses amd, matlab/rchol/find_separator.m:6):
+// 1 = METIS_NodeND, 2 = minimum degree (least degree in the elimination
+// graph first, ties by lowest index, neighbours joined into a clique).
+std::vector<uint64_t> leaf_order_of(const Csr &A, int mode) {
+  const int64_t n = A.n;
+  std::vector<uint64_t> p(n);
+  for (int64_t i = 0; i < n; ++i) p[i] = (uint64_t)i;
+  if (mode == 0 || n <= 2) return p;
+  if (mode == 1) {
+    idx_t N = n;
+    std::vector<idx_t> xadj(A.rp.begin(), A.rp.end()), adj(A.ci.begin(), A.ci.end()), perm(n), iperm(n);
+    if (adj.empty()) adj.push_back(0);
+    METIS_NodeND(&N, xadj.data(), adj.data(), nullptr, nullptr, perm.data(), iperm.data());
+    for (int64_t i = 0; i < n; ++i) p[i] = (uint64_t)perm[i];
+    return p;
+  }
+  std::vector<std::set<int64_t>> nb(n);
+  for (int64_t i = 0; i < n; ++i)
+    for (uint64_t j = A.rp[i]; j < A.rp[i + 1]; ++j)
+      if ((int64_t)A.ci[j] != i) nb[i].insert((int64_t)A.ci[j]);
+  std::vector<char> gone(n, 0);
+  for (int64_t k = 0; k < n; ++k) {
+    int64_t v = -1;
+    for (int64_t i = 0; i < n; ++i)  // least degree, lowest index
+      if (!gone[i] && (v < 0 || nb[i].size() < nb[v].size())) v = i;
+    p[k] = (uint64_t)v;
+    gone[v] = 1;
+    std::vector<int64_t> N(nb[v].begin(), nb[v].end());
+    for (int64_t u : N) {
+      nb[u].erase(v);
+      for (int64_t w : N)
+        if (w != u) nb[u].insert(w);
+    }
+    nb[v].clear();
+  }
+  return p;
+}
+
 void find_sep(const Csr &A, int depth, int target, std::vector<uint64_t> &p,
-              std::vector<uint64_t> &val, bool last_in_root = false) {
+              std::vector<uint64_t> &val, bool last_in_root = false, int leaf = 0) {
   if (depth == target) {
     val.assign(1, (uint64_t)A.n);
-    p.resize(A.n);
-    for (int64_t i = 0; i < A.n; ++i) p[i] = (uint64_t)i;
+    p = leaf_order_of(A, leaf);
     return;
   }
   if (A.n <= 1) throw std::invalid_argument("too many threads requested");
@@ -447,8 +486,8 @@ void find_sep(const Csr &A, int depth, int target, std::vector<uint64_t> &p,
   }
   Csr L = submatrix(l, sep, A), R = submatrix(r, sep, A);
   std::vector<uint64_t> pl, vl, pr, vr;
-  find_sep(L, depth + 1, target, pl, vl);
-  find_sep(R, depth + 1, target, pr, vr);
+  find_sep(L, depth + 1, target, pl, vl, false, leaf);
+  find_sep(R, depth + 1, target, pr, vr, false, leaf);
   val = vl;
   val.insert(val.end(), vr.begin(), vr.end());
   val.push_back(s.size());
@@ -655,7 +694,9 @@ int oracle_reorder(int64_t n, const uint64_t *rp, const uint64_t *ci, const doub
 
 // c++/rchol/rchol_parallel.cpp:37-70: remove the diagonal, nested dissection
 // to depth log2(threads)+1, result_idx with the ground vertex in the root.
-int oracle_order_ex(int64_t n, const uint64_t *rp, const uint64_t *ci, int threads, int last_in_root,
+// flags: 1 = last vertex in the root separator (Python front end), 2 = leaf
+// order METIS_NodeND, 4 = leaf order minimum degree.
+int oracle_order_ex(int64_t n, const uint64_t *rp, const uint64_t *ci, int threads, int flags,
                     uint64_t **perm, uint64_t **ridx, int64_t *nridx) {
   try {
     if (threads <= 0) throw std::invalid_argument("thread number should be positive");
@@ -672,7 +713,7 @@ int oracle_order_ex(int64_t n, const uint64_t *rp, const uint64_t *ci, int threa
     int target = 1;
     while ((1 << (target - 1)) < threads) ++target;
     std::vector<uint64_t> p, val;
-    find_sep(A, 1, target, p, val, last_in_root != 0);
+    find_sep(A, 1, target, p, val, (flags & 1) != 0, (flags & 2) ? 1 : (flags & 4) ? 2 : 0);
     std::vector<uint64_t> ri{0};
     for (uint64_t x : val) ri.push_back(ri.back() + x);
     ri.back() += 1;

@@ -11,6 +11,8 @@ extern "C" {
 int METIS_ComputeVertexSeparator(idx_t *nvtxs, idx_t *xadj, idx_t *adjncy,
                                  idx_t *vwgt, idx_t *options, idx_t *sepsize,
                                  idx_t *part);
+int METIS_NodeND(idx_t *nvtxs, idx_t *xadj, idx_t *adjncy, idx_t *vwgt, idx_t *options,
+                 idx_t *perm, idx_t *iperm);
 #ifdef __cplusplus
 }
 #endif

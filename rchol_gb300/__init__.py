@@ -48,7 +48,8 @@ def _csr(A):
     return A
 
 
-def rchol(A, nt=1, perm=np.array([]), part=np.array([]), seed=0, precision="fp64", order="python"):
+def rchol(A, nt=1, perm=np.array([]), part=np.array([]), seed=0, precision="fp64", order="python",
+          leaf_order="natural"):
     """Randomized Cholesky preconditioner of an SDDM matrix on the GPU.
 
     Mirrors python/rchol/rchol.py:8-45.  ``nt`` is the number of leaf
@@ -57,8 +58,11 @@ def rchol(A, nt=1, perm=np.array([]), part=np.array([]), seed=0, precision="fp64
     given together.  ``order="python"`` is the Python front end's nested
     dissection (the last vertex goes into the root separator,
     python/rchol_lap/find_separator.pyx:27-28), ``"c++"`` the C++ front
-    end's.  Returns ``(G, perm, part)`` with G lower triangular such that
-    G G^T approximates A[perm][:, perm].
+    end's.  ``leaf_order`` ("natural", "nd", "md") reorders inside the leaf
+    subdomains as the MATLAB front end does with amd
+    (matlab/rchol/find_separator.m:6): less fill, usually more PCG
+    iterations.  Returns ``(G, perm, part)`` with G lower triangular such
+    that G G^T approximates A[perm][:, perm].
     """
     if order not in ("python", "c++"):
         raise ValueError("order must be 'python' or 'c++'")
@@ -73,7 +77,7 @@ def rchol(A, nt=1, perm=np.array([]), part=np.array([]), seed=0, precision="fp64
         print("number of threads rounded down to {}".format(nt))
     A = _csr(A)
     if perm.size == 0:
-        tree = Tree.build(A.indptr, A.indices, nt, last_in_root=(order == "python"))
+        tree = Tree.build(A.indptr, A.indices, nt, last_in_root=(order == "python"), leaf_order=leaf_order)
     else:
         tree = Tree.from_partition(perm, part)
     perm, part = tree.arrays()

@@ -135,13 +135,15 @@ class Tree(Handle):
     _destroy = "rchol_gpu_tree_destroy"
 
     @classmethod
-    def build(cls, rowptr, colidx, threads, last_in_root=False):
+    def build(cls, rowptr, colidx, threads, last_in_root=False, leaf_order="natural"):
         """Nested dissection with ``threads`` leaves; ``last_in_root`` gives the
-        Python front end's variant (last vertex in the root separator)."""
+        Python front end's variant (last vertex in the root separator);
+        ``leaf_order`` = "natural" (C++ front end), "nd" (METIS nested
+        dissection inside leaves) or "md" (minimum degree inside leaves)."""
         rp, ci = i64(rowptr), i64(colidx)
+        flags = (1 if last_in_root else 0) | {"natural": 0, "nd": 2, "md": 4}[leaf_order]
         out = _vp()
-        check(lib().rchol_gpu_tree_build_ex(len(rp) - 1, p64(rp), p64(ci), int(threads), 1 if last_in_root else 0,
-                                            C.byref(out)))
+        check(lib().rchol_gpu_tree_build_ex(len(rp) - 1, p64(rp), p64(ci), int(threads), flags, C.byref(out)))
         return cls(out)
 
     @classmethod

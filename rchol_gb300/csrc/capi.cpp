@@ -82,9 +82,13 @@ int rchol_gpu_tree_build_ex(int64_t n, const int64_t *row_ptr, const int64_t *co
                             rchol_tree_t *out) {
   API_BEGIN
   RCHOL_CHECK_ARG(out, "null output handle");
-  RCHOL_CHECK_ARG((flags & ~RCHOL_ORDER_LAST_IN_ROOT) == 0, "unknown ordering flags");
+  RCHOL_CHECK_ARG((flags & ~(RCHOL_ORDER_LAST_IN_ROOT | RCHOL_ORDER_LEAF_ND | RCHOL_ORDER_LEAF_MD)) == 0,
+                  "unknown ordering flags");
+  RCHOL_CHECK_ARG(!((flags & RCHOL_ORDER_LEAF_ND) && (flags & RCHOL_ORDER_LEAF_MD)), "choose one leaf ordering");
   *out = nullptr;
-  *out = build_tree(n, row_ptr, col_idx, threads, (flags & RCHOL_ORDER_LAST_IN_ROOT) != 0);
+  const int leaf = (flags & RCHOL_ORDER_LEAF_ND) ? RCHOL_LEAF_ND : (flags & RCHOL_ORDER_LEAF_MD) ? RCHOL_LEAF_MD
+                                                                                                   : RCHOL_LEAF_NATURAL;
+  *out = build_tree(n, row_ptr, col_idx, threads, (flags & RCHOL_ORDER_LAST_IN_ROOT) != 0, leaf);
   API_END
 }
 

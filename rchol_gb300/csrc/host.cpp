@@ -11,6 +11,7 @@
 #include <memory>
 #include <future>
 #include <numeric>
+#include <set>
 #include <thread>
 
 #include <errno.h>
@@ -25,6 +26,8 @@
 extern "C" int METIS_ComputeVertexSeparator(int64_t *nvtxs, int64_t *xadj, int64_t *adjncy,
                                             int64_t *vwgt, int64_t *options, int64_t *sepsize,
                                             int64_t *part);
+extern "C" int METIS_NodeND(int64_t *nvtxs, int64_t *xadj, int64_t *adjncy, int64_t *vwgt, int64_t *options,
+                            int64_t *perm, int64_t *iperm);
 
 namespace rchol {
 
@@ -86,6 +89,56 @@ Graph subgraph(const std::vector<int64_t> &par, const std::vector<int64_t> &labe
   return s;
 }
 
+// Order inside a leaf subdomain.  The C++ front end keeps the natural order
+// (c++/rchol/find_separator.cpp:111-120); the MATLAB front end reorders every
+// leaf with a fill-reducing ordering (matlab/rchol/find_separator.m:6, amd).
+// Here: METIS nested dissection (METIS_NodeND) or a plain minimum-degree
+// ordering (below).  Both change only the order inside leaves.
+std::vector<int64_t> leaf_permutation(const Graph &g, int leaf_order) {
+  const int64_t n = g.n;
+  std::vector<int64_t> p(n);
+  std::iota(p.begin(), p.end(), 0);
+  if (leaf_order == RCHOL_LEAF_NATURAL || n <= 2) return p;
+  if (leaf_order == RCHOL_LEAF_ND) {
+    int64_t N = n;
+    std::vector<int64_t> xadj(g.xadj), adj(g.adj), perm(n), iperm(n);
+    if (adj.empty()) adj.push_back(0);
+    int rc = METIS_NodeND(&N, xadj.data(), adj.data(), nullptr, nullptr, perm.data(), iperm.data());
+    if (rc != 1) throw Error(RCHOL_ERR_INTERNAL, "METIS_NodeND failed");
+    return perm;  // position i holds vertex perm[i]
+  }
+  // minimum degree: eliminate a vertex of least degree in the elimination
+  // graph (ties: lowest index); its neighbours become a clique
+  std::vector<std::vector<int64_t>> nb(n);
+  std::set<std::pair<int64_t, int64_t>> q;
+  for (int64_t i = 0; i < n; ++i) {
+    for (int64_t j = g.xadj[i]; j < g.xadj[i + 1]; ++j)
+      if (g.adj[j] != i) nb[i].push_back(g.adj[j]);
+    std::sort(nb[i].begin(), nb[i].end());
+    nb[i].erase(std::unique(nb[i].begin(), nb[i].end()), nb[i].end());
+    q.insert({(int64_t)nb[i].size(), i});
+  }
+  int64_t k = 0;
+  std::vector<int64_t> merged;
+  while (!q.empty()) {
+    const int64_t v = q.begin()->second;
+    q.erase(q.begin());
+    p[k++] = v;
+    const std::vector<int64_t> N = std::move(nb[v]);
+    nb[v].clear();
+    for (int64_t u : N) {
+      q.erase({(int64_t)nb[u].size(), u});
+      merged.clear();
+      std::set_union(nb[u].begin(), nb[u].end(), N.begin(), N.end(), std::back_inserter(merged));
+      merged.erase(std::remove_if(merged.begin(), merged.end(), [&](int64_t x) { return x == u || x == v; }),
+                   merged.end());
+      nb[u].swap(merged);
+      q.insert({(int64_t)nb[u].size(), u});
+    }
+  }
+  return p;
+}
+
 // Number of partition segments below a node `levels` tree levels tall.
 int64_t segments(int levels) { return ((int64_t)1 << levels) - 1; }
 
@@ -101,9 +154,10 @@ int64_t segments(int levels) { return ((int64_t)1 << levels) - 1; }
 // mapping and exits without touching anything else.  Each METIS call sees
 // exactly the subgraph the serial recursion would give it, so the ordering is
 // identical to the serial one.
-void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks, bool last_in_root = false);
+void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks, bool last_in_root = false,
+             int leaf_order = RCHOL_LEAF_NATURAL);
 
-bool dissect_in_child(Graph &g, int depth, int target, int64_t *p, int64_t *val, int forks,
+bool dissect_in_child(Graph &g, int depth, int target, int64_t *p, int64_t *val, int forks, int leaf_order,
                       pid_t *pid_out, int64_t **shm_out, size_t *shm_bytes) {
   const int64_t nseg = segments(target - depth + 1);
   size_t bytes = (size_t)(1 + g.n + nseg) * sizeof(int64_t);
@@ -119,7 +173,7 @@ bool dissect_in_child(Graph &g, int depth, int target, int64_t *p, int64_t *val,
   if (pid == 0) {
     int64_t status = 2;
     try {
-      dissect(std::move(g), depth, target, shm + 1, shm + 1 + g.n, forks);
+      dissect(std::move(g), depth, target, shm + 1, shm + 1 + g.n, forks, false, leaf_order);
       status = 0;
     } catch (const Error &e) {
       status = e.status == RCHOL_ERR_INVALID ? 1 : 2;
@@ -152,10 +206,12 @@ void collect_child(pid_t pid, int64_t *shm, size_t bytes, int64_t n, int64_t nse
 
 // last_in_root: the Python front end's variant, which puts the last vertex
 // into the root separator (python/rchol_lap/find_separator.pyx:27-28).
-void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks, bool last_in_root) {
+void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks, bool last_in_root,
+             int leaf_order) {
   if (depth == target) {
     val[0] = g.n;
-    for (int64_t i = 0; i < g.n; ++i) p[i] = i;
+    const std::vector<int64_t> lp = leaf_permutation(g, leaf_order);
+    std::copy(lp.begin(), lp.end(), p);
     return;
   }
   if (g.n <= 1) throw Error(RCHOL_ERR_INVALID, "too many threads requested");
@@ -177,12 +233,12 @@ void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks
   int64_t *shm = nullptr;
   size_t shm_bytes = 0;
   bool forked = forks > 0 && gr.n >= 20000 &&
-                dissect_in_child(gr, depth + 1, target, pr.data(), vr.data(), forks - 1, &pid, &shm,
+                dissect_in_child(gr, depth + 1, target, pr.data(), vr.data(), forks - 1, leaf_order, &pid, &shm,
                                  &shm_bytes);
   if (forked) {
     gr = Graph();  // the child owns its copy
     try {
-      dissect(std::move(gl), depth + 1, target, pl.data(), vl.data(), forks - 1);
+      dissect(std::move(gl), depth + 1, target, pl.data(), vl.data(), forks - 1, false, leaf_order);
     } catch (...) {
       try {
         collect_child(pid, shm, shm_bytes, (int64_t)pr.size(), nseg, pr.data(), vr.data());
@@ -192,8 +248,8 @@ void dissect(Graph g, int depth, int target, int64_t *p, int64_t *val, int forks
     }
     collect_child(pid, shm, shm_bytes, (int64_t)pr.size(), nseg, pr.data(), vr.data());
   } else {
-    dissect(std::move(gl), depth + 1, target, pl.data(), vl.data(), forks - 1);
-    dissect(std::move(gr), depth + 1, target, pr.data(), vr.data(), forks - 1);
+    dissect(std::move(gl), depth + 1, target, pl.data(), vl.data(), forks - 1, false, leaf_order);
+    dissect(std::move(gr), depth + 1, target, pr.data(), vr.data(), forks - 1, false, leaf_order);
   }
   int64_t o = 0;
   for (int64_t x : vl) val[o++] = x;
@@ -240,7 +296,8 @@ void validate_csr(int64_t n, const int64_t *rp, const int64_t *ci) {
   }
 }
 
-rchol_tree_s *build_tree(int64_t n, const int64_t *rp, const int64_t *ci, int threads, bool last_in_root) {
+rchol_tree_s *build_tree(int64_t n, const int64_t *rp, const int64_t *ci, int threads, bool last_in_root,
+                         int leaf_order) {
   RCHOL_CHECK_ARG(threads > 0, "thread number should be positive");
   RCHOL_CHECK_ARG((threads & (threads - 1)) == 0, "thread number should be a power of 2");
   validate_csr(n, rp, ci);
@@ -251,7 +308,7 @@ rchol_tree_s *build_tree(int64_t n, const int64_t *rp, const int64_t *ci, int th
     int target = 1;
     while ((1 << (target - 1)) < threads) ++target;
     std::vector<int64_t> val;
-    if (target == 1) {
+    if (target == 1 && leaf_order == RCHOL_LEAF_NATURAL) {
       t->perm.resize(n);
       std::iota(t->perm.begin(), t->perm.end(), 0);
       val.assign(1, n);
@@ -278,7 +335,7 @@ rchol_tree_s *build_tree(int64_t n, const int64_t *rp, const int64_t *ci, int th
       if (const char *e = getenv("RCHOL_ORDER_FORK_LEVELS")) forks = atoi(e);
       t->perm.resize(n);
       val.resize(segments(target));
-      dissect(std::move(g), 1, target, t->perm.data(), val.data(), forks, last_in_root);
+      dissect(std::move(g), 1, target, t->perm.data(), val.data(), forks, last_in_root, leaf_order);
     }
     t->part.assign(1, 0);
     for (int64_t x : val) t->part.push_back(t->part.back() + x);

@@ -53,6 +53,33 @@ def test_ordering_python_variant_matches_reference_fixture(O, R):
         assert np.array_equal(po.astype(np.int64), g["perm_" + case]), case
 
 
+@pytest.mark.parametrize("leaf_order", ["nd", "md"])
+@pytest.mark.parametrize("n,threads", [(8, 1), (10, 2), (12, 8)])
+def test_leaf_orderings_bit_exact_and_fill_reducing(O, R, n, threads, leaf_order):
+    """Fill-reducing order inside the leaves (the MATLAB front end's amd step,
+    matlab/rchol/find_separator.m:6): host and oracle agree bit for bit, the
+    separators are untouched, and the factor has less fill than with the
+    natural leaf order."""
+    import oracle
+
+    A = R.laplace_3d(n)
+    Au = csr_u64(A)
+    perm, part = R.Tree.build(A.indptr, A.indices, threads, leaf_order=leaf_order).arrays()
+    po, ro = O.order(Au, threads, leaf_order=leaf_order)
+    assert np.array_equal(perm, po.astype(np.int64)) and np.array_equal(part, ro.astype(np.int64))
+    nat, part0 = R.Tree.build(A.indptr, A.indices, threads).arrays()
+    assert np.array_equal(part, part0)
+    for a, b in zip(part[:-1], part[1:]):  # same vertex set per segment
+        b = min(b, A.shape[0])
+        assert np.array_equal(np.sort(perm[a:b]), np.sort(nat[a:b]))
+    fill = {}
+    for name, p_ in (("natural", nat), (leaf_order, perm)):
+        Ap = O.reorder(Au, p_.astype(np.uint64))
+        G, d, _ = O.factor(O.extend(Ap), part.astype(np.uint64), oracle.MODE_DEVICE, 3)
+        fill[name] = len(G[1])
+    assert fill[leaf_order] < fill["natural"], fill
+
+
 def test_ordering_forked_workers_match_serial(O, R, monkeypatch):
     """Large enough that subtrees go to forked worker processes."""
     A = R.laplace_3d(40)
