@@ -57,18 +57,6 @@ struct StreamDir {
   int64_t steps = 0;                 // sequential block steps on the critical path
 };
 
-// Older per-row level schedule, still used for several right-hand sides.
-struct DirPlan {
-  std::vector<int> stage_ptr;
-  std::vector<int> stage_maxrows;
-  DevBuf<int64_t> nb, ne;
-  DevBuf<int64_t> lvl_off;
-  DevBuf<int64_t> level_ptr;
-  DevBuf<int32_t> rows;
-  DevBuf<int32_t> split;
-  int64_t crit_levels = 0;
-};
-
 // Workspace and captured CUDA graph of one PCG iteration for a given matrix
 // and number of right-hand sides (solve.cu).
 struct PcgWork {
@@ -116,15 +104,10 @@ struct SolvePlan {
   std::mutex lock;  // solves on one factor are serialised (they share workspaces)
   std::vector<std::unique_ptr<PcgWork>> pcg;
   std::vector<std::unique_ptr<SegWork>> seg;
-  DirPlan fwd, bwd;
   StreamDir sfwd, sbwd;
   StreamDir kfwd, kbwd;    // pieces for up to 32 right-hand sides (built on first use)
   bool kbuilt = false;
-  DevBuf<double> dinv;
-  DevBuf<float> dinv32;
-  int64_t dag_fwd = 0, dag_bwd = 0;
-  DevBuf<double> scratch;  // global fallback of the multi-RHS solve
-  DevBuf<float> scratch32;
+  int64_t dag_fwd = -1, dag_bwd = -1;  // dependency-chain lengths, computed on request
   DevBuf<double> ytmp;     // intermediate of precond (FP64 path)
   DevBuf<float> ytmp32;    // intermediate of precond (FP32 path)
   DevBuf<double> acc64;    // external partial sums of split stages

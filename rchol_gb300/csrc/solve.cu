@@ -1,24 +1,10 @@
-// Triangular solves with G, SpMV with A and the PCG loop of
-// c++/util/pcg.cpp:57-159 on the GPU.
+// SpMV with A, the transposed copy and FP32 copy of G, the solve plan, and
+// the PCG loops of c++/util/pcg.cpp:57-159 on the GPU (one system with k
+// right-hand sides, and many independent systems at once).  The triangular
+// solves themselves are in trsv.cu.
 //
-// Triangular solves.  G comes from a nested-dissection elimination, so row i
-// of G only references columns in i's own tree node or in its descendants.
-// The forward solve y = G^-1 r walks the tree from the leaves to the root, the
-// backward solve z = G^-T y from the root to the leaves; all nodes of one depth
-// are independent and go in one launch, one thread block per node.  Inside a
-// node the block
-//   A. streams every row's entries that point outside the node (already
-//      solved) and forms the partial right-hand side (bandwidth bound);
-//   B. solves the node's own triangular block level by level (rows of a level
-//      are independent), keeping the node's unknowns in shared memory;
-//   C. writes the node's unknowns out.
-// Levels, the row split between A and B, and 1/G_ii are precomputed per
-// factor (SolvePlan).  Values are FP64 or, for an FP32 factor, FP32 with FP32
-// accumulation ("applied in FP32"); the right-hand side comes in as FP64 and
-// the result leaves as FP64.
-//
-// Several right-hand sides are stored row-major (n x k) and solved in one
-// traversal: lanes then run over the right-hand sides of a row.
+// Several right-hand sides are stored row-major (n x k); every right-hand
+// side keeps its own PCG scalars and stopping test.
 
 #include <algorithm>
 #include <cmath>
@@ -37,150 +23,6 @@ void exclusive_scan_i64(int64_t *d_data, int64_t n, cudaStream_t s);
 void destroy_plan(SolvePlan *p) { delete p; }
 
 namespace {
-
-constexpr int TRSV_THREADS = 256;
-constexpr size_t TRSV_SMEM = 96 * 1024;
-
-template <typename VT>
-struct TrsvArgs {
-  const int64_t *rp;
-  const int32_t *ci;
-  const VT *val;
-  const VT *dinv;
-  const int64_t *nb, *ne, *lvl_off, *level_ptr;
-  const int32_t *rows, *split;
-  int node0;
-  int k;
-  bool upper;  // false: forward with L (external = leading), true: backward with U (trailing)
-  int64_t smem_rows;
-  VT *scratch;
-};
-
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-template <typename VT, typename InT, typename OutT>
-__global__ void __launch_bounds__(TRSV_THREADS) trsv_stage_kernel(TrsvArgs<VT> a, const InT *in, OutT *out) {
-  extern __shared__ unsigned char smem_raw[];
-  const int node = a.node0 + blockIdx.x;
-  const int64_t b = a.nb[node], e = a.ne[node];
-  const int64_t size = e - b;
-  if (size <= 0) return;
-  const int k = a.k;
-  VT *xs = (size <= a.smem_rows) ? reinterpret_cast<VT *>(smem_raw) : a.scratch + b * k;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-
-  // ---- A: right-hand side minus the external part ----------------------------
-  for (int64_t i = b + warp; i < e; i += nw) {
-    const int64_t r0 = a.rp[i], r1 = a.rp[i + 1];
-    int64_t x0, x1;  // external entry range
-    if (!a.upper) {
-      x0 = r0;
-      x1 = r0 + a.split[i];
-    } else {
-      x0 = r0 + a.split[i];
-      x1 = r1;
-    }
-    if (k == 1) {
-      VT s = 0;
-      for (int64_t q = x0 + lane; q < x1; q += 32) s += a.val[q] * (VT)out[a.ci[q]];
-      s = warp_sum(s);
-      if (lane == 0) xs[i - b] = (VT)in[i] - s;
-    } else {
-      for (int r = lane; r < k; r += 32) {
-        VT s = 0;
-        for (int64_t q = x0; q < x1; ++q) s += a.val[q] * (VT)out[(int64_t)a.ci[q] * k + r];
-        xs[(i - b) * k + r] = (VT)in[i * k + r] - s;
-      }
-    }
-  }
-  __syncthreads();
-  // ---- B: the node's own triangle, level by level ---------------------------
-  // level boundaries of this node: level_ptr[l0 .. l1] (the last one is the end)
-  const int64_t l0 = a.lvl_off[node], l1 = a.lvl_off[node + 1] - 1;
-  for (int64_t lv = l0; lv < l1; ++lv) {
-    const int64_t p0 = a.level_ptr[lv], p1 = a.level_ptr[lv + 1];
-    for (int64_t p = p0 + warp; p < p1; p += nw) {
-      const int64_t i = a.rows[p];
-      const int64_t r0 = a.rp[i], r1 = a.rp[i + 1];
-      int64_t q0, q1;  // internal off-diagonal entries
-      if (!a.upper) {
-        q0 = r0 + a.split[i];
-        q1 = r1 - 1;  // the diagonal is last
-      } else {
-        q0 = r0 + 1;  // the diagonal is first
-        q1 = r0 + a.split[i];
-      }
-      if (k == 1) {
-        VT s = 0;
-        for (int64_t q = q0 + lane; q < q1; q += 32) s += a.val[q] * xs[a.ci[q] - b];
-        s = warp_sum(s);
-        if (lane == 0) xs[i - b] = (xs[i - b] - s) * a.dinv[i];
-      } else {
-        for (int r = lane; r < k; r += 32) {
-          VT s = 0;
-          for (int64_t q = q0; q < q1; ++q) s += a.val[q] * xs[(int64_t)(a.ci[q] - b) * k + r];
-          xs[(i - b) * k + r] = (xs[(i - b) * k + r] - s) * a.dinv[i];
-        }
-      }
-    }
-    __syncthreads();
-  }
-  // ---- C: write the node's unknowns -------------------------------------------
-  for (int64_t t = threadIdx.x; t < size * k; t += blockDim.x) out[b * k + t] = (OutT)xs[t];
-}
-
-template <typename VT, typename InT, typename OutT>
-void run_trsv(const rchol_factor_s &F, const SolvePlan &P, bool upper, const InT *in, OutT *out,
-              int k, cudaStream_t s) {
-  const DirPlan &D = upper ? P.bwd : P.fwd;
-  TrsvArgs<VT> a;
-  if (!upper) {
-    a.rp = F.lrp.p;
-    a.ci = F.lci.p;
-  } else {
-    a.rp = F.urp.p;
-    a.ci = F.uci.p;
-  }
-  if constexpr (sizeof(VT) == 8) {
-    a.val = reinterpret_cast<const VT *>(upper ? F.uv.p : F.lv.p);
-    a.dinv = reinterpret_cast<const VT *>(P.dinv.p);
-    a.scratch = reinterpret_cast<VT *>(P.scratch.p);
-  } else {
-    a.val = reinterpret_cast<const VT *>(upper ? F.uv32.p : F.lv32.p);
-    a.dinv = reinterpret_cast<const VT *>(P.dinv32.p);
-    a.scratch = reinterpret_cast<VT *>(P.scratch32.p);
-  }
-  a.nb = D.nb.p;
-  a.ne = D.ne.p;
-  a.lvl_off = D.lvl_off.p;
-  a.level_ptr = D.level_ptr.p;
-  a.rows = D.rows.p;
-  a.split = D.split.p;
-  a.k = k;
-  a.upper = upper;
-  a.smem_rows = (int64_t)(TRSV_SMEM / (sizeof(VT) * (size_t)k));
-  static bool attr_set = false;
-  if (!attr_set) {
-    RCHOL_CUDA(cudaFuncSetAttribute(trsv_stage_kernel<VT, InT, OutT>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRSV_SMEM));
-    attr_set = true;
-  }
-  for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
-    int nodes = D.stage_ptr[st + 1] - D.stage_ptr[st];
-    if (!nodes) continue;
-    a.node0 = D.stage_ptr[st];
-    int64_t maxrows = D.stage_maxrows[st];
-    size_t smem = (size_t)std::min<int64_t>(maxrows, a.smem_rows) * sizeof(VT) * k;
-    trsv_stage_kernel<VT, InT, OutT><<<nodes, TRSV_THREADS, smem, s>>>(a, in, out);
-    note_launch();
-    RCHOL_CUDA(cudaGetLastError());
-  }
-}
 
 // ---- SpMV ---------------------------------------------------------------------
 
@@ -459,136 +301,6 @@ __global__ void init_kernel(int64_t nk, const double *b, double *x, double *r) {
 
 // ---- plan construction -----------------------------------------------------------
 
-static void build_dir(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, int64_t n,
-                      const std::vector<TreeNode> &nodes, bool upper, DirPlan &D, int64_t &dag,
-                      cudaStream_t s) {
-  // node order: forward = deepest first, backward = root first
-  int maxdepth = 1;
-  for (auto &nd : nodes) maxdepth = std::max(maxdepth, nd.depth);
-  std::vector<int> order;
-  D.stage_ptr.assign(1, 0);
-  D.stage_maxrows.clear();
-  for (int st = 0; st < maxdepth; ++st) {
-    int depth = upper ? st + 1 : maxdepth - st;
-    int64_t mr = 0;
-    for (size_t k = 0; k < nodes.size(); ++k)
-      if (nodes[k].depth == depth) {
-        order.push_back((int)k);
-        mr = std::max(mr, std::min(nodes[k].end, n) - nodes[k].begin);
-      }
-    D.stage_ptr.push_back((int)order.size());
-    D.stage_maxrows.push_back((int)mr);
-  }
-  const int nn = (int)order.size();
-  std::vector<int64_t> nb(nn), ne(nn);
-  for (int k = 0; k < nn; ++k) {
-    nb[k] = nodes[order[k]].begin;
-    ne[k] = std::min(nodes[order[k]].end, n);
-    if (ne[k] < nb[k]) ne[k] = nb[k];
-  }
-  std::vector<int32_t> split(n), level(n, 0), rows(n);
-  std::vector<int64_t> nlev(nn, 0);
-  // split and levels per node (independent across nodes)
-  parallel_for(nn, [&](int64_t k0, int64_t k1) {
-    for (int64_t k = k0; k < k1; ++k) {
-      int64_t b = nb[k], e = ne[k];
-      int64_t ml = -1;
-      if (!upper) {
-        for (int64_t i = b; i < e; ++i) {
-          int64_t q = rp[i], q1 = rp[i + 1] - 1;
-          while (q < q1 && ci[q] < b) ++q;
-          split[i] = (int32_t)(q - rp[i]);
-          int lv = 0;
-          for (; q < q1; ++q) lv = std::max(lv, level[ci[q]] + 1);
-          level[i] = lv;
-          ml = std::max<int64_t>(ml, lv);
-        }
-      } else {
-        for (int64_t i = e - 1; i >= b; --i) {
-          int64_t q = rp[i] + 1, q1 = rp[i + 1];
-          int lv = 0;
-          for (; q < q1 && ci[q] < e; ++q) lv = std::max(lv, level[ci[q]] + 1);
-          split[i] = (int32_t)(q - rp[i]);
-          level[i] = lv;
-          ml = std::max<int64_t>(ml, lv);
-        }
-      }
-      nlev[k] = ml + 1;
-    }
-  }, 1);
-  std::vector<int64_t> lvl_off(nn + 1, 0);
-  for (int k = 0; k < nn; ++k) lvl_off[k + 1] = lvl_off[k] + nlev[k];
-  std::vector<int64_t> level_ptr(lvl_off[nn] + 1, 0);
-  // counting sort of each node's rows by level (rows of a node are contiguous)
-  parallel_for(nn, [&](int64_t k0, int64_t k1) {
-    for (int64_t k = k0; k < k1; ++k) {
-      int64_t b = nb[k], e = ne[k], L = nlev[k];
-      std::vector<int64_t> cnt(L + 1, 0);
-      for (int64_t i = b; i < e; ++i) cnt[level[i] + 1]++;
-      for (int64_t l = 0; l < L; ++l) cnt[l + 1] += cnt[l];
-      for (int64_t l = 0; l < L; ++l) level_ptr[lvl_off[k] + l] = b + cnt[l];
-      std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
-      for (int64_t i = b; i < e; ++i) rows[b + pos[level[i]]++] = (int32_t)i;
-    }
-  }, 1);
-  // the level_ptr entry after a node's last level is the next node's first
-  // (or n); fill the closing entries per node
-  {
-    std::vector<int64_t> lp(lvl_off[nn] + nn + 1);
-    // re-pack with explicit end markers: node k levels at [lvl_off[k]+k, ...]
-    std::vector<int64_t> off2(nn + 1, 0);
-    for (int k = 0; k < nn; ++k) off2[k + 1] = off2[k] + nlev[k] + 1;
-    for (int k = 0; k < nn; ++k) {
-      for (int64_t l = 0; l < nlev[k]; ++l) lp[off2[k] + l] = level_ptr[lvl_off[k] + l];
-      lp[off2[k] + nlev[k]] = ne[k];
-    }
-    // lvl_off now indexes level starts; node k has levels [off2[k], off2[k+1]-1)
-    std::vector<int64_t> lo(nn + 1);
-    for (int k = 0; k <= nn; ++k) lo[k] = off2[k];
-    level_ptr.swap(lp);
-    lvl_off.swap(lo);
-  }
-  int64_t crit = 0;
-  for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
-    int64_t m = 0;
-    for (int k = D.stage_ptr[st]; k < D.stage_ptr[st + 1]; ++k) m = std::max(m, nlev[k]);
-    crit += m;
-  }
-  D.crit_levels = crit;
-  // DAG depth of the whole solve (for reporting)
-  {
-    std::vector<int32_t> lv(n, 0);
-    int32_t mx = 0;
-    if (!upper) {
-      for (int64_t i = 0; i < n; ++i) {
-        int32_t l = 0;
-        for (int64_t q = rp[i]; q < rp[i + 1] - 1; ++q) l = std::max(l, lv[ci[q]] + 1);
-        lv[i] = l;
-        mx = std::max(mx, l);
-      }
-    } else {
-      for (int64_t i = n - 1; i >= 0; --i) {
-        int32_t l = 0;
-        for (int64_t q = rp[i] + 1; q < rp[i + 1]; ++q) l = std::max(l, lv[ci[q]] + 1);
-        lv[i] = l;
-        mx = std::max(mx, l);
-      }
-    }
-    dag = (int64_t)mx + 1;
-  }
-  D.nb.upload(nb.data(), nn, s);
-  D.ne.upload(ne.data(), nn, s);
-  // lvl_off for the kernel: node k has levels [lvl_off[k], lvl_off[k+1]-1)
-  // (the last entry of each node's range is its end marker)
-  std::vector<int64_t> lo_kernel(nn + 1);
-  for (int k = 0; k <= nn; ++k) lo_kernel[k] = lvl_off[k];
-  D.lvl_off.upload(lo_kernel.data(), nn + 1, s);
-  D.level_ptr.upload(level_ptr.data(), level_ptr.size(), s);
-  D.rows.upload(rows.data(), n, s);
-  D.split.upload(split.data(), n, s);
-  RCHOL_CUDA(cudaStreamSynchronize(s));
-}
-
 namespace {
 
 __global__ void transpose_count_kernel(int64_t nnz, const int32_t *uci, unsigned long long *cnt) {
@@ -626,13 +338,6 @@ __global__ void row_sort_kernel(int64_t n, const int64_t *lrp, const int32_t *tc
   }
 }
 
-__global__ void diag_inverse_kernel(int64_t n, const int64_t *urp, const double *uv, double *dinv,
-                                    float *dinv32, const float *uv32) {
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  dinv[i] = 1.0 / uv[urp[i]];
-  if (dinv32) dinv32[i] = 1.0f / uv32[urp[i]];
-}
 
 __global__ void to_f32_kernel(int64_t n, const double *a, float *b) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -689,23 +394,6 @@ void build_plan(rchol_factor_s &F, cudaStream_t s) {
   const int64_t n = F.n, nnz = F.nnz;
   auto P = new SolvePlan();
   try {
-    std::vector<int64_t> rp(n + 1);
-    std::vector<int32_t> ci(nnz);
-    F.lrp.download(rp.data(), n + 1, s);
-    F.lci.download(ci.data(), nnz, s);
-    RCHOL_CUDA(cudaStreamSynchronize(s));
-    build_dir(rp, ci, n, F.nodes, false, P->fwd, P->dag_fwd, s);
-    F.urp.download(rp.data(), n + 1, s);
-    F.uci.download(ci.data(), nnz, s);
-    RCHOL_CUDA(cudaStreamSynchronize(s));
-    build_dir(rp, ci, n, F.nodes, true, P->bwd, P->dag_bwd, s);
-    P->dinv.alloc(n);
-    if (F.precision == RCHOL_PREC_FP32) P->dinv32.alloc(n);
-    diag_inverse_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
-        n, F.urp.p, F.uv.p, P->dinv.p, P->dinv32.p, F.uv32.p);
-    note_launch();
-    RCHOL_CUDA(cudaGetLastError());
-    RCHOL_CUDA(cudaStreamSynchronize(s));
     build_streams(F, *P, s);
   } catch (...) {
     delete P;
@@ -721,10 +409,8 @@ void build_plan(rchol_factor_s &F, cudaStream_t s) {
 static void ensure_scratch(SolvePlan &P, bool fp32, int64_t count) {
   bool grew = false;
   if (fp32) {
-    if (P.scratch32.n < (size_t)count) P.scratch32.alloc(count), grew = true;
     if (P.ytmp32.n < (size_t)count) P.ytmp32.alloc(count), grew = true;
   } else {
-    if (P.scratch.n < (size_t)count) P.scratch.alloc(count), grew = true;
     if (P.ytmp.n < (size_t)count) P.ytmp.alloc(count), grew = true;
   }
   if (grew) {
@@ -803,8 +489,38 @@ void edge_grad(int64_t m, const int64_t *ei, const int64_t *ej, const double *la
   RCHOL_CUDA(cudaGetLastError());
 }
 
+// Longest dependency chain (levels of a level schedule) of the forward or
+// backward solve, computed on first request from the CSR of G or G^T.
 int64_t plan_levels(const rchol_factor_s &F, bool upper) {
-  return upper ? F.plan->dag_bwd : F.plan->dag_fwd;
+  SolvePlan &P = *F.plan;
+  std::lock_guard<std::mutex> guard(P.lock);
+  int64_t &dag = upper ? P.dag_bwd : P.dag_fwd;
+  if (dag >= 0) return dag;
+  const int64_t n = F.n, nnz = F.nnz;
+  std::vector<int64_t> rp(n + 1);
+  std::vector<int32_t> ci(nnz);
+  (upper ? F.urp : F.lrp).download(rp.data(), n + 1, 0);
+  (upper ? F.uci : F.lci).download(ci.data(), nnz, 0);
+  RCHOL_CUDA(cudaStreamSynchronize(0));
+  std::vector<int32_t> lv(n, 0);
+  int32_t mx = 0;
+  if (!upper) {  // rows of G: diagonal last
+    for (int64_t i = 0; i < n; ++i) {
+      int32_t l = 0;
+      for (int64_t q = rp[i]; q < rp[i + 1] - 1; ++q) l = std::max(l, lv[ci[q]] + 1);
+      lv[i] = l;
+      mx = std::max(mx, l);
+    }
+  } else {  // rows of G^T: diagonal first
+    for (int64_t i = n - 1; i >= 0; --i) {
+      int32_t l = 0;
+      for (int64_t q = rp[i] + 1; q < rp[i + 1]; ++q) l = std::max(l, lv[ci[q]] + 1);
+      lv[i] = l;
+      mx = std::max(mx, l);
+    }
+  }
+  dag = n ? (int64_t)mx + 1 : 0;
+  return dag;
 }
 
 // PCG for k right-hand sides (device pointers), c++/util/pcg.cpp:57-127.
