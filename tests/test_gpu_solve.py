@@ -221,3 +221,21 @@ def test_fp32_preconditioner(case, O, R):
     zo = O.precond(G, r)
     err = np.linalg.norm(dz.cpu().numpy() - zo) / np.linalg.norm(zo)
     assert err < 1e-3, f"fp32 preconditioner relative error {err:.2e}"
+
+
+def test_factor_levels_report_dependency_depth(case):
+    """rchol_gpu_factor_levels: the longest dependency chain of the forward
+    (rows of G) and backward (rows of G^T) solves, against a host count."""
+    Gt_rp, Gt_ci = case["G"][0].astype(np.int64), case["G"][1].astype(np.int64)
+    n = len(Gt_rp) - 1
+    fwd, bwd = case["F"].levels()
+    lv = np.zeros(n, dtype=np.int64)  # backward: row i of G^T depends on its later columns
+    for i in range(n - 1, -1, -1):
+        cols = Gt_ci[Gt_rp[i] + 1:Gt_rp[i + 1]]
+        lv[i] = lv[cols].max() + 1 if cols.size else 0
+    assert bwd == lv.max() + 1
+    lf = np.zeros(n, dtype=np.int64)  # forward: column j of G^T feeds rows > j
+    for j in range(n):
+        rows = Gt_ci[Gt_rp[j] + 1:Gt_rp[j + 1]]
+        lf[rows] = np.maximum(lf[rows], lf[j] + 1)
+    assert fwd == lf.max() + 1
