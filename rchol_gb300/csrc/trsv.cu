@@ -14,13 +14,17 @@
 // forward solve, root first for the backward one).  A node larger than shared
 // memory is cut into pieces solved one after another.  Per stage:
 //   ext_kernel    acc_i = rhs_i - sum of row i's entries outside its piece
-//                 (columns already solved); one thread per row, all SMs.
-//   block_kernel  one warp per piece: the piece's unknowns live in the warp's
-//                 shared memory, block records stream in through a cp.async
-//                 double buffer, and per block lane r forms
+//                 (columns already solved), all SMs; 1, 4, 8 or 32 lanes per
+//                 row (ext_lanes_kernel) by the stage's mean row length.
+//   team_kernel   one thread block per piece (default): the piece's unknowns
+//                 live in shared memory, block records stream in through a
+//                 cp.async ring; warp 0 solves block k (near entries from the
+//                 previous block by shuffles, then the dense inverse) while
+//                 the helper warps sum the far entries of block k + 1:
 //                   t_r = acc_r - sum_{earlier blocks} G_rj x_j   (sparse)
 //                   x_r = sum_c (T^-1)_{rc} t_c                   (dense, 32 shuffles)
-//                 no block-wide barrier anywhere.
+//   block_kernel  one warp per piece, the same arithmetic without helpers
+//                 (depths whose blocks are too dense for the team ring).
 // Values are FP32 or FP64 as the factor is stored; the block inverses are
 // computed in FP64 on the host and rounded to the stored precision.
 
