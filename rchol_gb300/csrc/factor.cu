@@ -53,6 +53,7 @@ struct ElimArgs {
   const int64_t *lrp;  // extended Laplacian, upper CSR
   const int32_t *lci;
   const double *lv;
+  int64_t lnnz;        // entries of lci / lv
   int64_t next;        // n + 1 (ground vertex = next - 1)
   const int64_t *node_begin;
   const int64_t *node_end;
@@ -107,6 +108,16 @@ __device__ __forceinline__ bool wless(double wa, uint32_t ra, double wb, uint32_
   return wa < wb || (wa == wb && ra < rb);
 }
 
+// A double as an unsigned integer with the same order (negative zero taken
+// as zero, so equal weights stay equal): compares then run on the integer
+// pipes, which GB300 has many more of than FP64 ones.
+__device__ __forceinline__ uint64_t wkey(double w) {
+  const uint64_t b = (uint64_t)__double_as_longlong(w == 0.0 ? 0.0 : w);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+constexpr unsigned GCHUNK = 256;  // entries of G a warp reserves at a time
+
 // In-place ascending sort of n records (key[i], val[i]) by one warp: a
 // bitonic network whose merges compare each element with its mirror, so
 // every comparator points the same way and the missing elements past n
@@ -119,11 +130,12 @@ __device__ void warp_bitonic_sort(K *key, V *val, int n, Less less) {
   int npow = 1;
   while (npow < n) npow <<= 1;
   const int half = npow >> 1;
-  for (int k = 2; k <= npow; k <<= 1) {
+  int lk = 1;  // log2(k)
+  for (int k = 2; k <= npow; k <<= 1, ++lk) {
     const int hk = k >> 1;
     for (int t = lane; t < half; t += 32) {  // mirror stage
-      const int blk = t / hk, o = t - blk * hk;
-      const int i = blk * k + o, j = blk * k + k - 1 - o;
+      const int blk = t >> (lk - 1), o = t & (hk - 1);
+      const int i = (blk << lk) + o, j = (blk << lk) + k - 1 - o;
       if (j < n && less(key[j], val[j], key[i], val[i])) {
         const K tk = key[i];
         key[i] = key[j];
@@ -134,9 +146,10 @@ __device__ void warp_bitonic_sort(K *key, V *val, int n, Less less) {
       }
     }
     __syncwarp();
-    for (int d = hk >> 1; d >= 1; d >>= 1) {  // half cleaners
+    for (int ld = lk - 2; ld >= 0; --ld) {  // half cleaners, distance d = 2^ld
+      const int d = 1 << ld;
       for (int t = lane; t < half; t += 32) {
-        const int i = (t / d) * 2 * d + (t % d), j = i + d;
+        const int i = ((t >> ld) << (ld + 1)) + (t & (d - 1)), j = i + d;
         if (j < n && less(key[j], val[j], key[i], val[i])) {
           const K tk = key[i];
           key[i] = key[j];
@@ -151,7 +164,88 @@ __device__ void warp_bitonic_sort(K *key, V *val, int n, Less less) {
   }
 }
 
-constexpr int RANK_SORT_MAX = 64;  // wider columns use the bitonic network
+// Rank sorts of up to 32 * PER records with unique keys: lane l owns records
+// l, l + 32, ..., and one pass over all keys (four loads in flight) counts,
+// for each of them, the keys that order before it; the record then moves to
+// its rank.  Keys: (row << 32 | source) for the merge order, (weight as
+// order-preserving bits, row) for the sampling order.
+template <int PER>
+__device__ __forceinline__ void rank_sort_rowsrc(const uint64_t *key, const double *val, int n, uint64_t *okey,
+                                                 double *oval, int lane) {
+  uint64_t mine[PER];
+  int rank[PER];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int e = lane + 32 * p;
+    mine[p] = e < n ? key[e] : 0;
+    rank[p] = 0;
+  }
+  int f = 0;
+  for (; f + 4 <= n; f += 4) {
+    const uint64_t k0 = key[f], k1 = key[f + 1], k2 = key[f + 2], k3 = key[f + 3];
+#pragma unroll
+    for (int p = 0; p < PER; ++p)
+      rank[p] += (int)(k0 < mine[p]) + (int)(k1 < mine[p]) + (int)(k2 < mine[p]) + (int)(k3 < mine[p]);
+  }
+  for (; f < n; ++f) {
+    const uint64_t k0 = key[f];
+#pragma unroll
+    for (int p = 0; p < PER; ++p) rank[p] += (int)(k0 < mine[p]);
+  }
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int e = lane + 32 * p;
+    if (e < n) {
+      okey[rank[p]] = mine[p];
+      oval[rank[p]] = val[e];
+    }
+  }
+}
+
+// wk: order-preserving weight bits; rows in the low 32 bits of row.
+template <int PER>
+__device__ __forceinline__ void rank_sort_weight(const uint64_t *wk, const uint64_t *row, const double *val, int n,
+                                                 uint64_t *orow, double *oval, int lane) {
+  uint64_t mw[PER];
+  uint32_t mr[PER];
+  int rank[PER];
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int e = lane + 32 * p;
+    mw[p] = e < n ? wk[e] : 0;
+    mr[p] = e < n ? (uint32_t)row[e] : 0;
+    rank[p] = 0;
+  }
+  auto before = [](uint64_t wf, uint32_t rf, uint64_t we, uint32_t re) {
+    return (int)((wf < we) | ((wf == we) & (rf < re)));
+  };
+  int f = 0;
+  for (; f + 4 <= n; f += 4) {
+    const uint64_t w0 = wk[f], w1 = wk[f + 1], w2 = wk[f + 2], w3 = wk[f + 3];
+    const uint32_t r0 = (uint32_t)row[f], r1 = (uint32_t)row[f + 1], r2 = (uint32_t)row[f + 2],
+                   r3 = (uint32_t)row[f + 3];
+#pragma unroll
+    for (int p = 0; p < PER; ++p)
+      rank[p] += before(w0, r0, mw[p], mr[p]) + before(w1, r1, mw[p], mr[p]) + before(w2, r2, mw[p], mr[p]) +
+                 before(w3, r3, mw[p], mr[p]);
+  }
+  for (; f < n; ++f) {
+    const uint64_t w0 = wk[f];
+    const uint32_t r0 = (uint32_t)row[f];
+#pragma unroll
+    for (int p = 0; p < PER; ++p) rank[p] += before(w0, r0, mw[p], mr[p]);
+  }
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int e = lane + 32 * p;
+    if (e < n) {
+      orow[rank[p]] = mr[p];
+      oval[rank[p]] = val[e];
+    }
+  }
+}
+
+constexpr int RANK_SORT_MAX = 128;  // wider columns use the bitonic network
 
 __global__ void eliminate_kernel(ElimArgs a) {
   extern __shared__ unsigned char smem_raw[];
@@ -171,11 +265,37 @@ __global__ void eliminate_kernel(ElimArgs a) {
 
   const int64_t ground = a.next - 1;
   const int64_t cb = a.node_begin[warp], ce = a.node_end[warp];
+  // The next column's static inputs (row range, fill slab, first 32 initial
+  // entries) are loaded one column ahead, so their latency overlaps the
+  // current column; only its fill count and records wait for the current one.
+  int64_t nx_r1 = a.lrp[cb], nx_r2 = a.lrp[cb + 1];
+  uint32_t nx_cap = a.fcap[cb];
+  int64_t nx_fb = a.fbase[cb];
+  int32_t nx_col = 0;
+  double nx_v = 0.0;
+  if (nx_r1 + lane < nx_r2) {
+    nx_col = a.lci[nx_r1 + lane];
+    nx_v = a.lv[nx_r1 + lane];
+  }
+  unsigned long long gcur = 0, gend = 0;  // lane 0: this warp's reserved run of G
   for (int64_t c = cb; c < ce; ++c) {
     // ---- 1. gather ----------------------------------------------------------
-    const int64_t r0 = a.lrp[c], r1 = a.lrp[c + 1];
+    const int64_t r0 = nx_r1, r1 = nx_r2;
+    const uint32_t cap = nx_cap;
+    const int64_t fb = nx_fb;
+    const int32_t pre_col = nx_col;
+    const double pre_v = nx_v;
+    if (c + 1 < ce) {  // rows of column c+1 start at r1; lci/lv reads stay inside the arrays
+      nx_r1 = r1;
+      nx_r2 = a.lrp[c + 2];
+      nx_cap = a.fcap[c + 1];
+      nx_fb = a.fbase[c + 1];
+      if (r1 + lane < a.lnnz) {
+        nx_col = a.lci[r1 + lane];
+        nx_v = a.lv[r1 + lane];
+      }
+    }
     uint32_t nfill = __ldcg(&a.fcnt[c]);
-    const uint32_t cap = a.fcap[c];
     if (nfill > cap) nfill = cap;  // overflow already flagged by the writer
     int ninit = 0;
     // initial entries: count kept ones with a ballot per 32-wide chunk
@@ -185,8 +305,8 @@ __global__ void eliminate_kernel(ElimArgs a) {
       int32_t col = 0;
       double v = 0.0;
       if (k < r1) {
-        col = a.lci[k];
-        v = a.lv[k];
+        col = k0 == r0 ? pre_col : a.lci[k];
+        v = k0 == r0 ? pre_v : a.lv[k];
         keep = (col != c) && !(col == ground && v < 0.0 && c != ground);
       }
       unsigned bal = __ballot_sync(0xffffffffu, keep);
@@ -197,7 +317,6 @@ __global__ void eliminate_kernel(ElimArgs a) {
       }
       ninit += __popc(bal);
     }
-    const int64_t fb = a.fbase[c];
     int total = ninit + (int)nfill;
     if (total > E) {
       if (lane == 0) atomicMax(&a.flags[FLAG_WIDTH], total);
@@ -212,14 +331,12 @@ __global__ void eliminate_kernel(ElimArgs a) {
     }
     __syncwarp();
     // ---- 2. sort by (row, source) and merge --------------------------------
-    if (total <= RANK_SORT_MAX) {
-      for (int e = lane; e < total; e += 32) {
-        uint64_t ke = akey[e];
-        int rank = 0;
-        for (int f = 0; f < total; ++f) rank += (akey[f] < ke);
-        bkey[rank] = ke;
-        bval[rank] = aval[e];
-      }
+    if (total <= 32) {
+      rank_sort_rowsrc<1>(akey, aval, total, bkey, bval, lane);
+    } else if (total <= 64) {
+      rank_sort_rowsrc<2>(akey, aval, total, bkey, bval, lane);
+    } else if (total <= RANK_SORT_MAX) {
+      rank_sort_rowsrc<4>(akey, aval, total, bkey, bval, lane);
     } else {
       warp_bitonic_sort(akey, aval, total,
                         [](uint64_t ka, double, uint64_t kb, double) { return ka < kb; });
@@ -251,14 +368,13 @@ __global__ void eliminate_kernel(ElimArgs a) {
     __syncwarp();
     // ---- 3. sort by (weight, row), prefix sum --------------------------------
     if (m <= RANK_SORT_MAX) {
-      for (int e = lane; e < m; e += 32) {
-        double we = aval[e];
-        uint32_t re = (uint32_t)akey[e];
-        int rank = 0;
-        for (int f = 0; f < m; ++f) rank += wless(aval[f], (uint32_t)akey[f], we, re);
-        bkey[rank] = re;
-        bval[rank] = we;
-      }
+      uint64_t *wk = reinterpret_cast<uint64_t *>(cs);  // cs is free until the prefix sum
+      for (int e = lane; e < m; e += 32) wk[e] = wkey(aval[e]);
+      __syncwarp();
+      if (m <= 32) rank_sort_weight<1>(wk, akey, aval, m, bkey, bval, lane);
+      else if (m <= 64) rank_sort_weight<2>(wk, akey, aval, m, bkey, bval, lane);
+      else rank_sort_weight<4>(wk, akey, aval, m, bkey, bval, lane);
+      __syncwarp();  // every lane's reads of wk end before the prefix sum reuses cs
     } else {
       for (int e = lane; e < m; e += 32) {
         bkey[e] = (uint32_t)akey[e];
@@ -321,7 +437,13 @@ __global__ void eliminate_kernel(ElimArgs a) {
       int cnt = 1 + m - (hasg ? 1 : 0);
       unsigned long long gs = 0;
       if (lane == 0) {
-        gs = atomicAdd(a.gtop, (unsigned long long)cnt);
+        if (gcur + (unsigned)cnt > gend) {
+          const unsigned long long take = max((unsigned)cnt, GCHUNK);
+          gcur = atomicAdd(a.gtop, take);
+          gend = gcur + take;
+        }
+        gs = gcur;
+        gcur += (unsigned)cnt;
         a.diag[c] = csum;
         if (!(csum > 0.0)) atomicOr(&a.flags[FLAG_SINGULAR], 1);
       }
@@ -425,7 +547,9 @@ void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t
     else if (coldepth[c] == 3) cap[c] = 512u;
     else cap[c] = 256u;
   }
-  int64_t gcap = std::max<int64_t>(ext.nnz() * 10, 1024);
+  // G entries: a generous multiple of the input, plus the runs a warp may
+  // leave partly unused (one per tree node)
+  int64_t gcap = std::max<int64_t>(ext.nnz() * 10, 1024) + (int64_t)nodes.size() * GCHUNK;
 
   cudaDeviceProp prop;
   int dev;
@@ -460,6 +584,7 @@ void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t
     args.lrp = lrp.p;
     args.lci = lci.p;
     args.lv = lv.p;
+    args.lnnz = ext.nnz();
     args.next = next;
     args.fcnt = fcnt.p;
     args.fcap = fcap.p;

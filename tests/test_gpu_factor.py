@@ -34,6 +34,9 @@ CASES = [
     ("weighted12_t16", lambda: generators.laplace_3d_weighted(12, sigma=1.0, seed=3), 16),
     ("grid2d_t8", lambda: generators.grid_2d_weighted(40, 33, "loguniform", shift=1e-4, dirichlet=False, seed=1), 8),
     ("checker16_t8", lambda: generators.checkerboard_3d(16, block=4), 8),
+    # separator columns of up to ~170 merged entries: every sort path (one,
+    # two and four records per lane, and the bitonic network past 128)
+    ("weighted64_t256", lambda: generators.laplace_3d_weighted(64, sigma=1.0, seed=2), 256),
 ]
 
 
