@@ -112,7 +112,8 @@ __device__ __forceinline__ bool wless(double wa, uint32_t ra, double wb, uint32_
 // as zero, so equal weights stay equal): compares then run on the integer
 // pipes, which GB300 has many more of than FP64 ones.
 __device__ __forceinline__ uint64_t wkey(double w) {
-  const uint64_t b = (uint64_t)__double_as_longlong(w == 0.0 ? 0.0 : w);
+  uint64_t b = (uint64_t)__double_as_longlong(w);
+  if (b == 0x8000000000000000ull) b = 0;
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
@@ -322,12 +323,18 @@ __global__ void eliminate_kernel(ElimArgs a) {
       if (lane == 0) atomicMax(&a.flags[FLAG_WIDTH], total);
       total = 0;  // skip the column; the host retries with wider buffers
     }
-    for (uint32_t f = lane; f < nfill && total; f += 32) {
-      const FillRec *rp = &a.frec[fb + f];
-      uint32_t row = __ldcg(&rp->row), src = __ldcg(&rp->src);
-      double w = __ldcg(&rp->w);
-      akey[ninit + f] = ((uint64_t)row << 32) | src;
-      aval[ninit + f] = w;
+    // fill records: one 16-byte load each, two per lane in flight
+    for (uint32_t f0 = lane; f0 < nfill && total; f0 += 64) {
+      const uint32_t f1 = f0 + 32;
+      const uint4 q0 = __ldcg(reinterpret_cast<const uint4 *>(a.frec + fb + f0));
+      uint4 q1 = make_uint4(0u, 0u, 0u, 0u);
+      if (f1 < nfill) q1 = __ldcg(reinterpret_cast<const uint4 *>(a.frec + fb + f1));
+      akey[ninit + f0] = ((uint64_t)q0.x << 32) | q0.y;  // {row, src, w}
+      aval[ninit + f0] = __hiloint2double((int)q0.w, (int)q0.z);
+      if (f1 < nfill) {
+        akey[ninit + f1] = ((uint64_t)q1.x << 32) | q1.y;
+        aval[ninit + f1] = __hiloint2double((int)q1.w, (int)q1.z);
+      }
     }
     __syncwarp();
     // ---- 2. sort by (row, source) and merge --------------------------------
@@ -346,24 +353,48 @@ __global__ void eliminate_kernel(ElimArgs a) {
       }
     }
     __syncwarp();
+    // Records e and e + 32 of a lane are merged together: the first record
+    // of each row (its head) sums the row's duplicates left to right, both
+    // heads' runs in one loop.
     int m = 0;
-    for (int e0 = 0; e0 < total; e0 += 32) {
-      int e = e0 + lane;
-      bool head = false;
-      uint32_t row = 0;
-      if (e < total) {
-        row = (uint32_t)(bkey[e] >> 32);
-        head = (e == 0) || ((uint32_t)(bkey[e - 1] >> 32) != row);
+    auto row_of = [&](int e) { return (uint32_t)(bkey[e] >> 32); };
+    for (int e0 = 0; e0 < total; e0 += 64) {
+      const int ea = e0 + lane, eb = ea + 32;
+      bool ha = false, hb = false;
+      uint32_t rowa = 0, rowb = 0;
+      if (ea < total) {
+        rowa = row_of(ea);
+        ha = (ea == 0) || (row_of(ea - 1) != rowa);
       }
-      unsigned bal = __ballot_sync(0xffffffffu, head);
-      int pos = m + __popc(bal & ((1u << lane) - 1u));
-      if (head) {
-        double s = bval[e];
-        for (int f = e + 1; f < total && (uint32_t)(bkey[f] >> 32) == row; ++f) s = __dadd_rn(s, bval[f]);
-        akey[pos] = row;  // rows ascending
-        aval[pos] = s;
+      if (eb < total) {
+        rowb = row_of(eb);
+        hb = row_of(eb - 1) != rowb;
       }
-      m += __popc(bal);
+      double sa = ha ? bval[ea] : 0.0, sb = hb ? bval[eb] : 0.0;
+      int fa = ea + 1, fb = eb + 1;
+      bool ga = ha, gb = hb;
+      while (ga || gb) {
+        if (ga) {
+          if (fa < total && row_of(fa) == rowa) sa = __dadd_rn(sa, bval[fa++]);
+          else ga = false;
+        }
+        if (gb) {
+          if (fb < total && row_of(fb) == rowb) sb = __dadd_rn(sb, bval[fb++]);
+          else gb = false;
+        }
+      }
+      const unsigned lt = (1u << lane) - 1u;
+      const unsigned bala = __ballot_sync(0xffffffffu, ha), balb = __ballot_sync(0xffffffffu, hb);
+      const int pa = m + __popc(bala & lt), pb = m + __popc(bala) + __popc(balb & lt);
+      if (ha) {
+        akey[pa] = rowa;  // rows ascending
+        aval[pa] = sa;
+      }
+      if (hb) {
+        akey[pb] = rowb;
+        aval[pb] = sb;
+      }
+      m += __popc(bala) + __popc(balb);
     }
     __syncwarp();
     // ---- 3. sort by (weight, row), prefix sum --------------------------------
@@ -387,48 +418,72 @@ __global__ void eliminate_kernel(ElimArgs a) {
                         });
     }
     __syncwarp();
+    // inclusive prefix sum in 32-wide chunks (Hillis-Steele inside a chunk,
+    // then the running carry), two chunks scanned side by side
     double carry = 0.0;
-    for (int e0 = 0; e0 < m; e0 += 32) {
-      int e = e0 + lane;
-      double v = (e < m) ? bval[e] : 0.0;
+    for (int e0 = 0; e0 < m; e0 += 64) {
+      const int ea = e0 + lane, eb = ea + 32;
+      double va = (ea < m) ? bval[ea] : 0.0, vb = (eb < m) ? bval[eb] : 0.0;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
-        double t = __shfl_up_sync(0xffffffffu, v, d);
-        if (lane >= d) v = __dadd_rn(t, v);
+        const double ta = __shfl_up_sync(0xffffffffu, va, d), tb = __shfl_up_sync(0xffffffffu, vb, d);
+        if (lane >= d) {
+          va = __dadd_rn(ta, va);
+          vb = __dadd_rn(tb, vb);
+        }
       }
-      double out = __dadd_rn(carry, v);
-      if (e < m) cs[e] = out;
-      int last = min(31, m - 1 - e0);
-      carry = __shfl_sync(0xffffffffu, out, last);
+      const double outa = __dadd_rn(carry, va);
+      if (ea < m) cs[ea] = outa;
+      const double ca = __shfl_sync(0xffffffffu, outa, min(31, m - 1 - e0));
+      const double outb = __dadd_rn(ca, vb);
+      if (eb < m) cs[eb] = outb;
+      carry = __shfl_sync(0xffffffffu, outb, min(31, max(0, m - 1 - e0 - 32)));
     }
     __syncwarp();
     const double csum = m ? cs[m - 1] : 0.0;
     // ---- 4. sample ----------------------------------------------------------
-    for (int i = lane; i < m - 1; i += 32) {
-      double u = uniform53(a.seed, (uint64_t)c, (uint32_t)i);
-      double tar = cs[i];
-      double span = __dsub_rn(csum, tar);
-      double r = __dadd_rn(__dmul_rn(u, span), tar);
-      int lo = i, hi = m;
-      while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (cs[mid] < r) lo = mid + 1;
-        else hi = mid;
+    // Edges i and i + 32 of a lane are drawn together (straight-line code,
+    // one search loop for both), so their latency chains overlap; the binary
+    // searches compare prefix sums as order-preserving integers.
+    for (int i0 = lane; i0 < m - 1; i0 += 64) {
+      const bool two = i0 + 32 < m - 1;
+      const int i1 = two ? i0 + 32 : i0;
+      const double u0 = uniform53(a.seed, (uint64_t)c, (uint32_t)i0);
+      const double u1 = uniform53(a.seed, (uint64_t)c, (uint32_t)i1);
+      const double tar0 = cs[i0], tar1 = cs[i1];
+      const double span0 = __dsub_rn(csum, tar0), span1 = __dsub_rn(csum, tar1);
+      const uint64_t r0 = wkey(__dadd_rn(__dmul_rn(u0, span0), tar0));
+      const uint64_t r1 = wkey(__dadd_rn(__dmul_rn(u1, span1), tar1));
+      int lo0 = i0, hi0 = m, lo1 = i1, hi1 = m;
+      while (lo0 < hi0 || lo1 < hi1) {
+        const int mid0 = (lo0 + hi0) >> 1, mid1 = (lo1 + hi1) >> 1;
+        const bool go0 = lo0 < hi0, go1 = lo1 < hi1;
+        const uint64_t c0 = wkey(cs[go0 ? mid0 : 0]), c1 = wkey(cs[go1 ? mid1 : 0]);
+        if (go0) {
+          if (c0 < r0) lo0 = mid0 + 1;
+          else hi0 = mid0;
+        }
+        if (go1) {
+          if (c1 < r1) lo1 = mid1 + 1;
+          else hi1 = mid1;
+        }
       }
-      int k = lo < m ? lo : m - 1;
-      if (k == i) continue;
-      double wn = __ddiv_rn(__dmul_rn(bval[i], span), csum);
-      uint32_t ri = (uint32_t)bkey[i], rk = (uint32_t)bkey[k];
-      uint32_t t = min(ri, rk), mx = max(ri, rk);
-      uint32_t slot = atomicAdd(&a.fcnt[t], 1u);
-      if (slot < a.fcap[t]) {
-        FillRec rec;
-        rec.row = mx;
-        rec.src = (uint32_t)c + 1u;
-        rec.w = wn;
-        a.frec[a.fbase[t] + slot] = rec;
-      } else {
-        atomicOr(&a.flags[FLAG_FILL], 1);
+      const int k0 = lo0 < m ? lo0 : m - 1, k1 = lo1 < m ? lo1 : m - 1;
+      const bool e0 = k0 != i0, e1 = two && k1 != i1;
+      const double w0 = __ddiv_rn(__dmul_rn(bval[i0], span0), csum);
+      const double w1 = __ddiv_rn(__dmul_rn(bval[i1], span1), csum);
+      const uint32_t ri0 = (uint32_t)bkey[i0], rk0 = (uint32_t)bkey[k0];
+      const uint32_t ri1 = (uint32_t)bkey[i1], rk1 = (uint32_t)bkey[k1];
+      const uint32_t t0 = min(ri0, rk0), x0 = max(ri0, rk0), t1 = min(ri1, rk1), x1 = max(ri1, rk1);
+      const uint32_t s0 = e0 ? atomicAdd(&a.fcnt[t0], 1u) : 0u;
+      const uint32_t s1 = e1 ? atomicAdd(&a.fcnt[t1], 1u) : 0u;
+      if (e0) {
+        if (s0 < a.fcap[t0]) a.frec[a.fbase[t0] + s0] = FillRec{x0, (uint32_t)c + 1u, w0};
+        else atomicOr(&a.flags[FLAG_FILL], 1);
+      }
+      if (e1) {
+        if (s1 < a.fcap[t1]) a.frec[a.fbase[t1] + s1] = FillRec{x1, (uint32_t)c + 1u, w1};
+        else atomicOr(&a.flags[FLAG_FILL], 1);
       }
     }
     // ---- 5. column of G -------------------------------------------------------
