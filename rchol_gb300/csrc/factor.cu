@@ -21,8 +21,10 @@
 // Per column (one warp, shared memory only):
 //   1. gather the initial entries (CSR row c of the upper extended Laplacian,
 //      minus the diagonal and negative ground edges) and the fill records;
-//   2. rank-sort by (row, source) and sum duplicate rows left to right;
-//   3. rank-sort by (weight, row), warp Hillis-Steele prefix sum;
+//   2. sort by (row, source) and sum duplicate rows left to right;
+//   3. sort by (weight, row), prefix sum in 32-wide Hillis-Steele chunks;
+//      (sorts: ranks in one pass over the keys up to 128 records, a bitonic
+//      network past that; the keys are unique, so both give one order)
 //   4. sample the m-1 fill edges in parallel, one lane per edge, with a
 //      Philox4x32-10 uniform keyed by (seed, c, i) and a binary search;
 //   5. write the column of G: sqrt(d) then -(w/d)*sqrt(d) per row.
