@@ -1,0 +1,311 @@
+// CPU check of the triangular-solve streams (test infrastructure only).
+//
+// Builds the forward (G) and backward (G^T) streams of a factor with the
+// library's own host-side builder (build_dir_streams, host copy, no device),
+// then executes them on the CPU in the order the kernels do: per stage the
+// external entries, then per piece block after block -- in the team format
+// the helpers' far sums of block k+1 from the unknowns solved before block k,
+// the solver's near entries from block k-1, and the packed inverse.  Every
+// column a record reads must already be solved at that point (a record that
+// reads ahead would race on the GPU); the results are compared with plain
+// substitution on the CSR of G.
+//
+//   stream_emulator <dir> <team_mode 0|1|2> <precision 0=FP64|1=FP32> <kwidth 1|32>
+//
+// <dir> holds hdr.bin (n, nnz, len(result_idx)), rp.bin / ci.bin / v.bin (CSR
+// of G^T: int64, int32, f64) and ridx.bin (result_idx, int64).  Prints one
+// line "ok rel_fwd rel_bwd team_pieces steps" or "FAIL ..." (exit code 1).
+
+#include "../rchol_gb300/csrc/trsv.cu"
+
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <functional>
+#include <string>
+
+namespace rchol {
+// the few library functions trsv.cu calls that live in other files
+int host_threads() { return 1; }
+void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)> &body, int64_t) { body(0, n); }
+void note_launch(int64_t) {}
+void set_last_error(const std::string &) {}
+}  // namespace rchol
+
+using namespace rchol;
+
+namespace {
+
+template <typename T>
+std::vector<T> read_file(const std::string &path, size_t n) {
+  std::vector<T> v(n);
+  std::ifstream f(path, std::ios::binary);
+  f.read(reinterpret_cast<char *>(v.data()), (std::streamsize)(n * sizeof(T)));
+  if (!f) {
+    std::printf("FAIL cannot read %s\n", path.c_str());
+    std::exit(1);
+  }
+  return v;
+}
+
+[[noreturn]] void fail(const char *what, long a, long b) {
+  std::printf("FAIL %s %ld %ld\n", what, a, b);
+  std::exit(1);
+}
+
+template <typename VT>
+VT ld(const unsigned char *p, size_t idx) {
+  VT x;
+  std::memcpy(&x, p + sizeof(VT) * idx, sizeof(VT));
+  return x;
+}
+
+uint32_t col_at(const unsigned char *p, size_t idx, uint32_t csz) {
+  if (csz == 2) {
+    uint16_t c;
+    std::memcpy(&c, p + 2 * idx, 2);
+    return c;
+  }
+  uint32_t c;
+  std::memcpy(&c, p + 4 * idx, 4);
+  return c;
+}
+
+// x = T^-1 t with the packed inverse of a record
+template <typename VT>
+void apply_inverse(const unsigned char *minv, const VT *t, VT *x, bool upper) {
+  for (int r = 0; r < BS; ++r) {
+    VT s = 0;
+    for (int c = 0; c < BS; ++c) {
+      const bool in = upper ? (r <= c) : (r >= c);
+      if (in) s += ld<VT>(minv, (size_t)tri_col_off(c, upper) + (size_t)(upper ? r : r - c)) * t[c];
+    }
+    x[r] = s;
+  }
+}
+
+template <typename VT>
+std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &rhs, int64_t n, bool upper,
+                            bool slot_major, long &team_pieces) {
+  std::vector<double> out(n, 0.0);
+  std::vector<char> done(n, 0);
+  const uint32_t vsz = sizeof(VT);
+  for (size_t st = 0; st + 1 < H.stage_ptr.size(); ++st) {
+    std::vector<VT> acc(n, 0);
+    // external entries: columns outside the piece, all solved in earlier stages
+    for (int k = H.stage_ptr[st]; k < H.stage_ptr[st + 1]; ++k) {
+      const NodeDesc &nd = H.desc[k];
+      for (int r = 0; r < nd.rows; ++r) {
+        const int64_t i = nd.begin + r;
+        VT s = 0;
+        for (int64_t q = H.ext_rp[i]; q < H.ext_rp[i + 1]; ++q) {
+          const int64_t c = H.ext_ci[q];
+          if (c < 0 || c >= n || !done[c]) fail("external column not yet solved", (long)c, (long)st);
+          s += (VT)H.ext_v[q] * (VT)out[c];
+        }
+        acc[i] = (VT)rhs[i] - s;
+      }
+    }
+    const bool team = H.stage_team[st] != 0;
+    for (int k = H.stage_ptr[st]; k < H.stage_ptr[st + 1]; ++k) {
+      const NodeDesc &nd = H.desc[k];
+      std::vector<VT> xs(nd.rows);
+      std::vector<int> solved_at(nd.rows, -1);  // block step that solved a piece row
+      for (int r = 0; r < nd.rows; ++r) xs[r] = acc[nd.begin + r];
+      auto rec = [&](int b) {
+        const int64_t o = H.blk_off[nd.blk0 + b];
+        if (o < 0 || o >= (int64_t)H.blocks.size()) fail("record offset", (long)o, b);
+        return H.blocks.data() + o;
+      };
+      if (!team) {
+        for (int b = 0; b < nd.nblocks; ++b) {
+          const unsigned char *p = rec(b);
+          uint32_t hdr[4];
+          std::memcpy(hdr, p, 16);
+          const uint32_t nr = hdr[0], nent = hdr[1], row0 = hdr[2], csz = hdr[3];
+          const size_t o_col = 16 + al16(4 * (BS + 1)), o_val = o_col + al16((size_t)csz * nent),
+                       o_min = o_val + al16((size_t)vsz * nent);
+          uint32_t off[BS + 1];
+          std::memcpy(off, p + 16, sizeof(off));
+          VT t[BS] = {}, x[BS];
+          for (uint32_t r = 0; r < nr; ++r) {
+            VT s = 0;
+            for (uint32_t e = off[r]; e < off[r + 1]; ++e) {
+              const uint32_t c = col_at(p + o_col, e, csz);
+              if (c >= (uint32_t)nd.rows || solved_at[c] < 0) fail("warp-format column not yet solved", c, b);
+              s += ld<VT>(p + o_val, e) * xs[c];
+            }
+            t[r] = xs[row0 + r] - s;
+          }
+          apply_inverse<VT>(p + o_min, t, x, upper);
+          for (uint32_t r = 0; r < nr; ++r) {
+            xs[row0 + r] = x[r];
+            solved_at[row0 + r] = b;
+          }
+        }
+      } else {
+        ++team_pieces;
+        std::vector<VT> u(2 * BS, (VT)NAN);  // u of blocks by parity, as the helpers leave it
+        VT xprev[BS] = {};
+        for (int b = 0; b < nd.nblocks; ++b) {
+          if (b + 1 < nd.nblocks) {  // helpers: far sums of block b+1 (columns solved before block b)
+            const unsigned char *p = rec(b + 1);
+            uint32_t h[16];
+            std::memcpy(h, p, 64);
+            const uint32_t nr1 = h[0], row01 = h[1], nchunk = h[4], clen = h[5], csz = h[6];
+            const TeamLayout L = team_layout(h[3], slot_major ? h[7] : 0, nchunk, clen, csz, vsz);
+            if ((int64_t)L.len != H.blk_off[nd.blk0 + b + 2] - H.blk_off[nd.blk0 + b + 1])
+              fail("team record length", (long)L.len, b + 1);
+            if (h[11] != L.o_fcol || h[12] != L.o_fval || h[13] != L.o_min) fail("team record offsets", b + 1, 0);
+            if ((int)nchunk > nd.maxchunk) fail("chunks above the piece's maximum", nchunk, nd.maxchunk);
+            std::vector<VT> part(nchunk);
+            for (uint32_t c = 0; c < nchunk; ++c) {
+              VT s0 = 0, s1 = 0;
+              for (uint32_t j = 0; j < clen; ++j) {
+                const size_t at = (size_t)j * nchunk + c;
+                const uint32_t col = col_at(p + L.o_fcol, at, csz);
+                const VT val = ld<VT>(p + L.o_fval, at);
+                if (col >= (uint32_t)nd.rows) fail("far column outside the piece", col, b + 1);
+                if (val != (VT)0 && (solved_at[col] < 0 || solved_at[col] > b - 1))
+                  fail("far column not solved before the step", col, b + 1);
+                (j & 1 ? s1 : s0) += val * xs[col];
+              }
+              part[c] = s0 + s1;
+            }
+            uint16_t crow[BS + 1];
+            std::memcpy(crow, p + L.o_crow, sizeof(crow));
+            if (crow[BS] != nchunk) fail("chunk rows", crow[BS], nchunk);
+            for (uint32_t r = 0; r < (uint32_t)BS; ++r) {
+              VT f0 = 0, f1 = 0;
+              for (uint32_t c = crow[r]; c < crow[r + 1]; ++c) ((c - crow[r]) & 1 ? f1 : f0) += part[c];
+              u[((b + 1) & 1) * BS + r] = r < nr1 ? xs[row01 + r] - (f0 + f1) : (VT)0;
+            }
+          }
+          // solver: block b, near entries from block b-1 (still in registers)
+          const unsigned char *p = rec(b);
+          uint32_t h[16];
+          std::memcpy(h, p, 64);
+          const uint32_t nr = h[0], row0 = h[1], prow0 = h[2], nmax = h[7];
+          const TeamLayout L = team_layout(h[3], slot_major ? nmax : 0, h[4], h[5], h[6], vsz);
+          uint16_t noff[BS + 1];
+          if (!slot_major) {
+            std::memcpy(noff, p + L.o_noff, sizeof(noff));
+            if (noff[BS] != h[3]) fail("near offsets", noff[BS], h[3]);
+          }
+          VT t[BS] = {}, x[BS];
+          for (uint32_t r = 0; r < nr; ++r) {
+            const VT ur = b == 0 ? xs[row0 + r] : u[(b & 1) * BS + r];
+            if (std::isnan((double)ur)) fail("u not prepared", r, b);
+            const uint32_t cnt = slot_major ? nmax : (uint32_t)(noff[r + 1] - noff[r]);
+            if (cnt > nmax) fail("near entries above nmax", r, b);
+            VT s0 = 0, s1 = 0;
+            for (uint32_t j = 0; j < cnt; ++j) {
+              const size_t at = slot_major ? (size_t)j * BS + r : (size_t)noff[r] + j;
+              const uint32_t c = p[L.o_ncol + at];
+              const VT val = ld<VT>(p + L.o_nval, at);
+              if (c >= (uint32_t)BS) fail("near column", c, b);
+              if (val != (VT)0 && (b == 0 || solved_at[prow0 + c] != b - 1)) fail("near column not in the previous block", c, b);
+              (j & 1 ? s1 : s0) += val * xprev[c];
+            }
+            t[r] = ur - (s0 + s1);
+          }
+          apply_inverse<VT>(p + L.o_min, t, x, upper);
+          for (int r = 0; r < BS; ++r) xprev[r] = r < (int)nr ? x[r] : (VT)0;
+          for (uint32_t r = 0; r < nr; ++r) {
+            xs[row0 + r] = x[r];
+            solved_at[row0 + r] = b;
+          }
+        }
+      }
+      for (int r = 0; r < nd.rows; ++r) {
+        if (solved_at[r] < 0) fail("piece row never solved", r, k);
+        out[nd.begin + r] = (double)xs[r];
+        done[nd.begin + r] = 1;
+      }
+    }
+  }
+  for (int64_t i = 0; i < n; ++i)
+    if (!done[i]) fail("row outside every piece", (long)i, 0);
+  return out;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  if (argc < 5) {
+    std::printf("FAIL usage: stream_emulator <dir> <team_mode> <precision> <kwidth>\n");
+    return 1;
+  }
+  const std::string dir = argv[1];
+  const int team_mode = std::atoi(argv[2]);
+  const bool fp32 = std::atoi(argv[3]) != 0;
+  const int kwidth = std::atoi(argv[4]);
+  const auto hdr = read_file<int64_t>(dir + "/hdr.bin", 3);
+  const int64_t n = hdr[0], nnz = hdr[1], nr = hdr[2];
+  const auto rp = read_file<int64_t>(dir + "/rp.bin", n + 1);
+  const auto ci = read_file<int32_t>(dir + "/ci.bin", nnz);
+  const auto v = read_file<double>(dir + "/v.bin", nnz);
+  const auto ri = read_file<int64_t>(dir + "/ridx.bin", nr);
+  // tree from result_idx: left half, right half, then the separator
+  // (rchol_lap.cpp:187-355)
+  std::vector<TreeNode> nodes;
+  std::function<void(int64_t, int64_t, int)> split = [&](int64_t start, int64_t total, int depth) {
+    if (total == 1) {
+      nodes.push_back({ri[start], std::min(ri[start + 1], n), depth, true});
+      return;
+    }
+    const int64_t half = (total - 1) / 2;
+    split(start, half, depth + 1);
+    split(start + half, half, depth + 1);
+    nodes.push_back({ri[start + total - 1], std::min(ri[start + total], n), depth, false});
+  };
+  split(0, nr - 1, 1);
+  // G (CSR of rows) = transpose of the CSR of G^T
+  std::vector<int64_t> lrp(n + 1, 0);
+  for (int32_t c : ci) lrp[c + 1]++;
+  for (int64_t i = 0; i < n; ++i) lrp[i + 1] += lrp[i];
+  std::vector<int32_t> lci(nnz);
+  std::vector<double> lv(nnz);
+  std::vector<int64_t> cur(lrp.begin(), lrp.end() - 1);
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t q = rp[i]; q < rp[i + 1]; ++q) {
+      const int64_t j = ci[q];
+      lci[cur[j]] = (int32_t)i;
+      lv[cur[j]++] = v[q];
+    }
+  // substitution references: y = G^-1 b, z = G^-T y
+  std::vector<double> b(n), y(n), z(n);
+  for (int64_t i = 0; i < n; ++i) b[i] = std::sin(0.37 * (double)i) + 0.1;
+  for (int64_t i = 0; i < n; ++i) {
+    double s = b[i], d = 0;
+    for (int64_t q = lrp[i]; q < lrp[i + 1]; ++q)
+      if (lci[q] == i) d = lv[q];
+      else s -= lv[q] * y[lci[q]];
+    y[i] = s / d;
+  }
+  for (int64_t i = n - 1; i >= 0; --i) {
+    double s = y[i], d = 0;
+    for (int64_t q = rp[i]; q < rp[i + 1]; ++q)
+      if (ci[q] == i) d = v[q];
+      else s -= v[q] * z[ci[q]];
+    z[i] = s / d;
+  }
+  StreamDir Df, Db;
+  HostStreamCopy Hf, Hb;
+  Df.team_warps = Db.team_warps = 8;
+  build_dir_streams(lrp, lci, lv, n, nodes, false, fp32, team_mode, kwidth, Df, 0, &Hf);
+  build_dir_streams(rp, ci, v, n, nodes, true, fp32, team_mode, kwidth, Db, 0, &Hb);
+  long tf = 0, tb = 0;
+  const bool slot_major = kwidth > 1;
+  const auto ye = fp32 ? emulate<float>(Hf, b, n, false, slot_major, tf) : emulate<double>(Hf, b, n, false, slot_major, tf);
+  const auto ze = fp32 ? emulate<float>(Hb, y, n, true, slot_major, tb) : emulate<double>(Hb, y, n, true, slot_major, tb);
+  double ey = 0, ny = 0, ez = 0, nz = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    ey += (ye[i] - y[i]) * (ye[i] - y[i]);
+    ny += y[i] * y[i];
+    ez += (ze[i] - z[i]) * (ze[i] - z[i]);
+    nz += z[i] * z[i];
+  }
+  std::printf("ok %.3e %.3e %ld %ld\n", std::sqrt(ey / ny), std::sqrt(ez / nz), tf + tb, (long)(Df.steps + Db.steps));
+  return 0;
+}

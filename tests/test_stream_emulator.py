@@ -1,0 +1,77 @@
+"""The triangular-solve streams, checked on the CPU.
+
+tests/stream_emulator.cu compiles the library's own stream builder (host
+code of rchol_gb300/csrc/trsv.cu) into a CPU program, builds the forward and
+backward streams of oracle factors (device-contract mode, i.e. the GPU's G)
+and executes them in the kernels' order: every record may only read unknowns
+solved at that point, and the result must equal plain substitution.  Warp,
+mixed and team formats, FP64 and FP32 values, single and 32-wide records."""
+
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from rchol_gb300 import generators
+from conftest import ROOT, csr_u64
+
+SCRATCH = os.path.join(ROOT, "tests", ".scratch")
+NVCC = shutil.which("nvcc") or ("/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else None)
+
+CASES = [
+    ("lap24_t16", lambda: generators.laplace_3d(24), 16),
+    ("weighted20_t8", lambda: generators.laplace_3d_weighted(20, sigma=1.0, seed=4), 8),
+    ("grid2d_t8", lambda: generators.grid_2d_weighted(70, 50, "loguniform", shift=1e-4, dirichlet=False, seed=2), 8),
+    ("checker16_t8", lambda: generators.checkerboard_3d(16, block=4), 8),
+]
+
+
+@pytest.fixture(scope="module")
+def emulator(built):
+    if NVCC is None:
+        pytest.skip("nvcc not available")
+    os.makedirs(SCRATCH, exist_ok=True)
+    exe = os.path.join(SCRATCH, "stream_emulator")
+    src = os.path.join(ROOT, "tests", "stream_emulator.cu")
+    deps = [src] + [os.path.join(ROOT, "rchol_gb300", "csrc", f) for f in ("trsv.cu", "plan.hpp", "common.hpp")]
+    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(d) for d in deps):
+        subprocess.run([NVCC, "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+                        "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "rchol_gb300", "csrc"),
+                        "-o", exe, src], check=True, capture_output=True)
+    return exe
+
+
+@pytest.fixture(scope="module", params=CASES, ids=[c[0] for c in CASES])
+def factor_dir(request, O):
+    name, make, threads = request.param
+    A = make()
+    G, perm, ridx, d = O.rchol(csr_u64(A), threads, seed=7, mode=oracle.MODE_DEVICE)
+    out = os.path.join(SCRATCH, name)
+    os.makedirs(out, exist_ok=True)
+    n = len(G[0]) - 1
+    np.array([n, len(G[1]), len(ridx)], np.int64).tofile(os.path.join(out, "hdr.bin"))
+    G[0].astype(np.int64).tofile(os.path.join(out, "rp.bin"))
+    G[1].astype(np.int32).tofile(os.path.join(out, "ci.bin"))
+    np.asarray(G[2], np.float64).tofile(os.path.join(out, "v.bin"))
+    np.asarray(ridx, np.int64).tofile(os.path.join(out, "ridx.bin"))
+    return out
+
+
+@pytest.mark.parametrize("team_mode,precision,kwidth", [(0, 0, 1), (1, 0, 1), (2, 0, 1), (2, 1, 1), (2, 0, 32),
+                                                         (2, 1, 32)],
+                         ids=["warp-fp64", "mixed-fp64", "team-fp64", "team-fp32", "wide-fp64", "wide-fp32"])
+def test_streams_solve_exactly(emulator, factor_dir, team_mode, precision, kwidth):
+    res = subprocess.run([emulator, factor_dir, str(team_mode), str(precision), str(kwidth)], capture_output=True,
+                         text=True, timeout=300)
+    line = res.stdout.strip().splitlines()[-1] if res.stdout.strip() else res.stderr
+    assert res.returncode == 0 and line.startswith("ok"), line
+    _, rel_fwd, rel_bwd, team_pieces, steps = line.split()
+    tol = 1e-12 if precision == 0 else 1e-4  # FP32 values and arithmetic
+    assert float(rel_fwd) < tol and float(rel_bwd) < tol, line
+    if team_mode == 2:
+        assert int(team_pieces) > 0
+    if team_mode == 0:
+        assert int(team_pieces) == 0
