@@ -941,7 +941,7 @@ static int sm_count() {
   return count;
 }
 
-// Host copy of one direction's stream (development checks decode it on the CPU).
+// Host copy of one direction's stream (tests/stream_emulator.cu executes it on the CPU).
 struct HostStreamCopy {
   std::vector<unsigned char> blocks;
   std::vector<int64_t> blk_off;
