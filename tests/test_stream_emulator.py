@@ -75,3 +75,23 @@ def test_streams_solve_exactly(emulator, factor_dir, team_mode, precision, kwidt
         assert int(team_pieces) > 0
     if team_mode == 0:
         assert int(team_pieces) == 0
+
+
+def test_emulator_catches_a_misordered_tree(emulator, O):
+    """Negative control, planted on the CPU: the boundary between two sibling
+    subdomains is moved so that rows of one read unknowns of the other in the
+    same stage; the emulator must refuse the streams."""
+    A = generators.laplace_3d(16)
+    G, perm, ridx, d = O.rchol(csr_u64(A), 4, seed=7, mode=oracle.MODE_DEVICE)
+    out = os.path.join(SCRATCH, "misordered")
+    os.makedirs(out, exist_ok=True)
+    n = len(G[0]) - 1
+    bad = np.asarray(ridx, np.int64).copy()
+    bad[1] -= 10  # the last 10 rows of the first subdomain now belong to its sibling
+    np.array([n, len(G[1]), len(bad)], np.int64).tofile(os.path.join(out, "hdr.bin"))
+    G[0].astype(np.int64).tofile(os.path.join(out, "rp.bin"))
+    G[1].astype(np.int32).tofile(os.path.join(out, "ci.bin"))
+    np.asarray(G[2], np.float64).tofile(os.path.join(out, "v.bin"))
+    bad.tofile(os.path.join(out, "ridx.bin"))
+    res = subprocess.run([emulator, out, "2", "0", "1"], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 1 and "not yet solved" in res.stdout, res.stdout
