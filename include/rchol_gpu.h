@@ -128,6 +128,11 @@ int rchol_gpu_factor_precision(rchol_factor_t G);
 int rchol_gpu_factor_export(rchol_factor_t G, int64_t *row_ptr, int64_t *col_idx, double *val);
 /* Pivots d of the factorization (length n), G = L sqrt(D). */
 int rchol_gpu_factor_pivots(rchol_factor_t G, double *d);
+/* Wall time (seconds) of the set-up phases that made G: the elimination
+ * kernels (0 for rchol_gpu_factor_from_host), the assembly of G (transpose,
+ * row sort, FP32 copies) and the triangular-solve plan.  No counterpart in
+ * the reference. */
+int rchol_gpu_factor_setup_times(rchol_factor_t G, double *eliminate_s, double *assemble_s, double *plan_s);
 /* Level-schedule depth of the forward and backward solves. */
 int rchol_gpu_factor_levels(rchol_factor_t G, int64_t *fwd_levels, int64_t *bwd_levels);
 void rchol_gpu_factor_destroy(rchol_factor_t G);
@@ -170,8 +175,9 @@ int rchol_gpu_precond_d(rchol_factor_t G, const double *d_r, double *d_z, int64_
  * that loads it until the process exits, so n is limited to 1,048,576 for an
  * FP64 factor and 2,097,152 for an FP32 one (larger n: RCHOL_ERR_INVALID).
  * The first call on a device looks up the array's device address (make it
- * before any stream capture).  All calls share the array: calls that overlap
- * on the GPU race.  Device pointers. */
+ * before any stream capture); later calls on a stream that is not capturing
+ * look it up again, so a device reset leaves no stale address.  All calls
+ * share the array: calls that overlap on the GPU race.  Device pointers. */
 int rchol_gpu_precond_noalloc_d(rchol_factor_t G, const double *d_r, double *d_z, void *stream);
 /* Forward (y = G^-1 r) or backward (z = G^-T y) solve alone; device pointers. */
 int rchol_gpu_trsv_d(rchol_factor_t G, int transpose, const double *d_in, double *d_out,

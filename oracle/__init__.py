@@ -27,15 +27,18 @@ _i64 = C.c_int64
 MODE_REF = 0
 MODE_DEVICE = 1
 
+# Where the reference sources live (only the development machine has them).
+REFERENCE_DIR = os.environ.get("RCHOL_REFERENCE_DIR", "/root/reference")
+
 
 def build(with_ref: bool | None = None) -> None:
     """Compile liboracle.so (and the reference library if its sources exist)."""
     targets = ["oracle"]
     if with_ref is None:
-        with_ref = os.path.isdir("/root/reference/c++")
+        with_ref = os.path.isdir(os.path.join(REFERENCE_DIR, "c++"))
     if with_ref:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-j8", *targets], cwd=HERE, check=True)
+    subprocess.run(["make", "-s", "-j8", *targets, f"RCHOL_REFERENCE_DIR={REFERENCE_DIR}"], cwd=HERE, check=True)
 
 
 def _p(a, t):

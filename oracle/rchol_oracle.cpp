@@ -27,17 +27,24 @@
 // a*b+c rounded twice, as the device code does with explicit _rn intrinsics.
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <future>
 #include <set>
 #include <random>
 #include <stdexcept>
 #include <string>
 #include <thread>
 #include <vector>
+
+#include <errno.h>
+#include <sys/mman.h>
+#include <sys/wait.h>
+#include <unistd.h>
 
 #include "shim/metis.h"
 
@@ -138,7 +145,8 @@ struct Factor {
   std::vector<double> diag;
   int mode;
   uint64_t seed;
-  bool singular = false;
+  std::atomic<bool> singular{false};
+  size_t par_depth = 0;  // MODE_REF: right children above this depth run on their own thread
 };
 
 // c++/rchol_lap/rchol_lap.cpp:794-813: column i from CSR row i of the upper
@@ -243,10 +251,23 @@ std::vector<FillEdge> tree_ref(Factor &F, const std::vector<uint64_t> &ri, size_
     for (uint64_t i = lb; i < rb; ++i) eliminate_ref(F, i, gen, defer, lb, rb);
     return defer;
   }
-  std::mt19937 rgen((std::mt19937::result_type)F.seed);
-  std::vector<FillEdge> r =
-      tree_ref(F, ri, depth + 1, (total - 1) / 2 + start, (total - 1) / 2, target, rgen);
-  std::vector<FillEdge> l = tree_ref(F, ri, depth + 1, start, (total - 1) / 2, target, gen);
+  // The two subtrees touch disjoint columns, so the right one may run on a
+  // thread of its own, as the reference's std::async does (near the root
+  // only, to bound the thread count); the streams and results are the same
+  // either way.
+  auto right = [&F, &ri, depth, start, total, target] {
+    std::mt19937 rgen((std::mt19937::result_type)F.seed);
+    return tree_ref(F, ri, depth + 1, (total - 1) / 2 + start, (total - 1) / 2, target, rgen);
+  };
+  std::vector<FillEdge> r, l;
+  if (depth <= F.par_depth) {
+    std::future<std::vector<FillEdge>> fr = std::async(std::launch::async, right);
+    l = tree_ref(F, ri, depth + 1, start, (total - 1) / 2, target, gen);
+    r = fr.get();
+  } else {
+    r = right();
+    l = tree_ref(F, ri, depth + 1, start, (total - 1) / 2, target, gen);
+  }
   uint64_t lb = ri[start + total - 1], rb = ri[start + total];
   for (const std::vector<FillEdge> *part : {&l, &r}) {
     for (const FillEdge &e : *part) {
@@ -469,7 +490,68 @@ std::vector<uint64_t> leaf_order_of(const Csr &A, int mode) {
 }
 
 void find_sep(const Csr &A, int depth, int target, std::vector<uint64_t> &p,
-              std::vector<uint64_t> &val, bool last_in_root = false, int leaf = 0) {
+              std::vector<uint64_t> &val, bool last_in_root = false, int leaf = 0, int forks = 0);
+
+// Orders subgraph R in a forked child process while the caller orders the
+// other half.  The METIS archive keeps its state in process globals, so
+// threads would perturb each other; a child has its own copy, and every
+// METIS call still sees exactly the subgraph of the serial recursion, so the
+// ordering is unchanged.  Returns false (nothing started) if fork fails.
+struct ForkedSep {
+  pid_t pid = -1;
+  uint64_t *shm = nullptr;
+  size_t bytes = 0;
+};
+
+bool fork_sep(const Csr &R, int depth, int target, int leaf, int forks, ForkedSep &f) {
+  const size_t nseg = ((size_t)1 << (target - depth + 1)) - 1;  // segments below `depth`
+  f.bytes = (2 + (size_t)R.n + nseg) * sizeof(uint64_t);
+  void *m = mmap(nullptr, f.bytes, PROT_READ | PROT_WRITE, MAP_SHARED | MAP_ANONYMOUS, -1, 0);
+  if (m == MAP_FAILED) return false;
+  f.shm = static_cast<uint64_t *>(m);
+  f.shm[0] = 2;  // status: 0 ok, 1 invalid argument, 2 failure
+  f.pid = fork();
+  if (f.pid < 0) {
+    munmap(m, f.bytes);
+    return false;
+  }
+  if (f.pid == 0) {
+    uint64_t st = 2;
+    try {
+      std::vector<uint64_t> pr, vr;
+      find_sep(R, depth, target, pr, vr, false, leaf, forks);
+      if (vr.size() <= nseg) {
+        std::memcpy(f.shm + 2, pr.data(), pr.size() * sizeof(uint64_t));
+        std::memcpy(f.shm + 2 + R.n, vr.data(), vr.size() * sizeof(uint64_t));
+        f.shm[1] = vr.size();
+        st = 0;
+      }
+    } catch (const std::invalid_argument &) {
+      st = 1;
+    } catch (...) {
+    }
+    f.shm[0] = st;
+    _exit(0);
+  }
+  return true;
+}
+
+void join_sep(ForkedSep &f, int64_t n, std::vector<uint64_t> &pr, std::vector<uint64_t> &vr) {
+  int st = 0;
+  while (waitpid(f.pid, &st, 0) < 0 && errno == EINTR) {
+  }
+  const uint64_t status = f.shm[0];
+  if (status == 0) {
+    pr.assign(f.shm + 2, f.shm + 2 + n);
+    vr.assign(f.shm + 2 + n, f.shm + 2 + n + f.shm[1]);
+  }
+  munmap(f.shm, f.bytes);
+  if (status == 1) throw std::invalid_argument("too many threads requested");
+  if (status != 0) throw std::runtime_error("ordering worker process failed");
+}
+
+void find_sep(const Csr &A, int depth, int target, std::vector<uint64_t> &p,
+              std::vector<uint64_t> &val, bool last_in_root, int leaf, int forks) {
   if (depth == target) {
     val.assign(1, (uint64_t)A.n);
     p = leaf_order_of(A, leaf);
@@ -486,8 +568,22 @@ void find_sep(const Csr &A, int depth, int target, std::vector<uint64_t> &p,
   }
   Csr L = submatrix(l, sep, A), R = submatrix(r, sep, A);
   std::vector<uint64_t> pl, vl, pr, vr;
-  find_sep(L, depth + 1, target, pl, vl, false, leaf);
-  find_sep(R, depth + 1, target, pr, vr, false, leaf);
+  ForkedSep f;
+  if (forks > 0 && R.n >= 20000 && fork_sep(R, depth + 1, target, leaf, forks - 1, f)) {
+    try {
+      find_sep(L, depth + 1, target, pl, vl, false, leaf, forks - 1);
+    } catch (...) {
+      try {
+        join_sep(f, R.n, pr, vr);
+      } catch (...) {
+      }
+      throw;
+    }
+    join_sep(f, R.n, pr, vr);
+  } else {
+    find_sep(L, depth + 1, target, pl, vl, false, leaf, forks);
+    find_sep(R, depth + 1, target, pr, vr, false, leaf, forks);
+  }
   val = vl;
   val.insert(val.end(), vr.begin(), vr.end());
   val.push_back(s.size());
@@ -713,7 +809,10 @@ int oracle_order_ex(int64_t n, const uint64_t *rp, const uint64_t *ci, int threa
     int target = 1;
     while ((1 << (target - 1)) < threads) ++target;
     std::vector<uint64_t> p, val;
-    find_sep(A, 1, target, p, val, (flags & 1) != 0, (flags & 2) ? 1 : (flags & 4) ? 2 : 0);
+    int forks = 0;  // levels of the recursion that order their right half in a child process
+    while ((1u << forks) < std::max(1u, std::thread::hardware_concurrency())) ++forks;
+    if (const char *e = std::getenv("ORACLE_ORDER_FORK_LEVELS")) forks = std::atoi(e);
+    find_sep(A, 1, target, p, val, (flags & 1) != 0, (flags & 2) ? 1 : (flags & 4) ? 2 : 0, forks);
     std::vector<uint64_t> ri{0};
     for (uint64_t x : val) ri.push_back(ri.back() + x);
     ri.back() += 1;
@@ -750,6 +849,8 @@ int oracle_factor(int64_t next, const uint64_t *rp, const uint64_t *ci, const do
       std::vector<uint64_t> ri(ridx, ridx + nridx);
       size_t threads = ri.size() / 2;
       size_t target = (size_t)(std::log2((double)threads) + 1);
+      const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+      F.par_depth = (size_t)std::log2((double)hw);  // about one thread per core
       std::mt19937 gen((std::mt19937::result_type)seed);
       tree_ref(F, ri, 1, 0, ri.size() - 1, target, gen);
     } else {

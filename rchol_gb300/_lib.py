@@ -49,6 +49,7 @@ SIGNATURES = [
     ("rchol_gpu_factor_export", C.c_int, [_vp, _i64p, _i64p, _dp]),
     ("rchol_gpu_factor_pivots", C.c_int, [_vp, _dp]),
     ("rchol_gpu_factor_levels", C.c_int, [_vp, _i64p, _i64p]),
+    ("rchol_gpu_factor_setup_times", C.c_int, [_vp, _dp, _dp, _dp]),
     ("rchol_gpu_factor_destroy", None, [_vp]),
     ("rchol_gpu_pcg", C.c_int, [_vp, _vp, _dp, _dp, _i64, C.c_double, C.c_int, _dp, _ip]),
     ("rchol_gpu_pcg_d", C.c_int, [_vp, _vp, _vp, _vp, _i64, C.c_double, C.c_int, _dp, _ip, _vp]),
@@ -249,3 +250,9 @@ class Factor(Handle):
         f, b = _i64(), _i64()
         check(lib().rchol_gpu_factor_levels(self.ptr, C.byref(f), C.byref(b)))
         return f.value, b.value
+
+    def setup_times(self):
+        """Seconds spent in elimination, assembly of G and the solve plan."""
+        e, a, p = C.c_double(), C.c_double(), C.c_double()
+        check(lib().rchol_gpu_factor_setup_times(self.ptr, C.byref(e), C.byref(a), C.byref(p)))
+        return {"eliminate": e.value, "assemble": a.value, "plan": p.value}

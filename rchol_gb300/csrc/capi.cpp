@@ -2,6 +2,7 @@
 // a status code and a thread-local message.
 
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <cstring>
 #include <memory>
@@ -212,7 +213,10 @@ int rchol_gpu_factor(rchol_matrix_t A, rchol_tree_t tree, uint64_t seed, int pre
   F->precision = precision;
   F->nodes = tree ? tree->nodes : trivial_nodes(A->n);
   cudaStream_t s = 0;
+  const auto t0 = std::chrono::steady_clock::now();
   gpu_factor(ext, F->nodes, seed, *F, s);
+  RCHOL_CUDA(cudaStreamSynchronize(s));
+  F->t_eliminate = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   finish_factor(*F, s);
   *out = F.release();
   API_END
@@ -248,6 +252,15 @@ int rchol_gpu_factor_from_host(int64_t n, const int64_t *row_ptr, const int64_t 
 }
 
 int64_t rchol_gpu_factor_nnz(rchol_factor_t G) { return G ? G->nnz : -1; }
+
+int rchol_gpu_factor_setup_times(rchol_factor_t G, double *eliminate_s, double *assemble_s, double *plan_s) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(G, "null factor");
+  if (eliminate_s) *eliminate_s = G->t_eliminate;
+  if (assemble_s) *assemble_s = G->t_assemble;
+  if (plan_s) *plan_s = G->t_plan;
+  API_END
+}
 int rchol_gpu_factor_precision(rchol_factor_t G) { return G ? G->precision : -1; }
 
 int rchol_gpu_factor_export(rchol_factor_t G, int64_t *row_ptr, int64_t *col_idx, double *val) {

@@ -154,5 +154,8 @@ struct rchol_factor_s {
   rchol::DevBuf<double> pivots;  // d (length n), when produced by the GPU factorization
   std::vector<rchol::TreeNode> nodes;
   rchol::SolvePlan *plan = nullptr;
+  // Wall time of the set-up phases (seconds): the elimination kernels, the
+  // assembly of G (transpose, row sort, FP32 copies) and the solve plan.
+  double t_eliminate = 0.0, t_assemble = 0.0, t_plan = 0.0;
   ~rchol_factor_s() { rchol::destroy_plan(plan); }
 };

@@ -7,6 +7,7 @@
 // side keeps its own PCG scalars and stopping test.
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -353,6 +354,7 @@ __global__ void i64_from_ull_kernel(int64_t n, const unsigned long long *a, int6
 
 void finish_factor(rchol_factor_s &F, cudaStream_t s) {
   const int64_t n = F.n, nnz = F.nnz;
+  const auto t0 = std::chrono::steady_clock::now();
   // L = transpose(U)
   DevBuf<unsigned long long> cnt(n);
   RCHOL_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), s));
@@ -387,7 +389,12 @@ void finish_factor(rchol_factor_s &F, cudaStream_t s) {
     note_launch();
     RCHOL_CUDA(cudaGetLastError());
   }
+  RCHOL_CUDA(cudaStreamSynchronize(s));
+  const auto t1 = std::chrono::steady_clock::now();
   build_plan(F, s);
+  RCHOL_CUDA(cudaStreamSynchronize(s));
+  F.t_assemble = std::chrono::duration<double>(t1 - t0).count();
+  F.t_plan = std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
 }
 
 void build_plan(rchol_factor_s &F, cudaStream_t s) {

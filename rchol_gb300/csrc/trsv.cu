@@ -31,6 +31,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "common.hpp"
@@ -1232,6 +1234,19 @@ void build_streams_k(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
 
 // ---- launch ------------------------------------------------------------------------------
 
+constexpr int kMaxDevices = 128;
+
+// A kernel's dynamic shared-memory limit above 48 KiB is an attribute of the
+// current device: `set` runs once per device ordinal (per flag array, i.e.
+// per kernel family), and concurrent first calls from several host threads
+// wait for the one that sets it.  A `set` that throws leaves the flag unset.
+template <typename Fn>
+static void once_per_device(std::once_flag (&flags)[kMaxDevices], Fn &&set) {
+  int dev = 0;
+  RCHOL_CUDA(cudaGetDevice(&dev));
+  RCHOL_CHECK_ARG(dev >= 0 && dev < kMaxDevices, "device ordinal out of range");
+  std::call_once(flags[dev], std::forward<Fn>(set));
+}
 
 template <typename VT, typename InT, typename OutT>
 static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *out, VT *acc, cudaStream_t s) {
@@ -1239,8 +1254,8 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
   constexpr bool f64 = sizeof(VT) == 8;
   const VT *ext_v = reinterpret_cast<const VT *>(f64 ? (const void *)D.ext_v64.p : (const void *)D.ext_v32.p);
   const int smem_cap = 220 * 1024;
-  static bool attr = false;
-  if (!attr) {
+  static std::once_flag attr_once[kMaxDevices];
+  once_per_device(attr_once, [&] {
     RCHOL_CUDA(cudaFuncSetAttribute(block_kernel<VT, OutT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     smem_cap));
     RCHOL_CUDA(cudaFuncSetAttribute(block_kernel<VT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1249,8 +1264,7 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
                                     smem_cap));
     RCHOL_CUDA(cudaFuncSetAttribute(team_kernel<VT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     smem_cap));
-    attr = true;
-  }
+  });
   BlockArgs<VT> a;
   a.nodes = D.nodes.p;
   a.blocks = D.blocks.p;
@@ -1350,14 +1364,13 @@ static void launch_streams_k(const SolvePlan &P, bool upper, const InT *in, OutT
   constexpr bool f64 = sizeof(VT) == 8;
   const VT *ext_v = reinterpret_cast<const VT *>(f64 ? (const void *)D.ext_v64.p : (const void *)D.ext_v32.p);
   const int smem_cap = 220 * 1024;
-  static bool attr = false;
-  if (!attr) {
+  static std::once_flag attr_once[kMaxDevices];
+  once_per_device(attr_once, [&] {
     RCHOL_CUDA(cudaFuncSetAttribute(team_k_kernel<VT, OutT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     smem_cap));
     RCHOL_CUDA(cudaFuncSetAttribute(team_k_kernel<VT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     smem_cap));
-    attr = true;
-  }
+  });
   TeamArgs<VT> ta;
   ta.nodes = D.nodes.p;
   ta.blocks = D.blocks.p;
@@ -1422,20 +1435,27 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 namespace {
 std::mutex g_noalloc_mutex;
-void *g_noalloc_ptr[128] = {};  // device address of the array, per device ordinal
+void *g_noalloc_ptr[kMaxDevices] = {};  // device address of the array, per device ordinal
 }  // namespace
 
 size_t noalloc_scratch_bytes() { return kNoAllocScratchBytes; }
 
 // Set-up on the current device: the array's host-side name is only a
-// stand-in, so the device address is looked up once per device (this first
-// call should therefore come before any stream capture).
-static void *noalloc_scratch_address() {
+// stand-in, so its device address is looked up with the device current.  The
+// first call on a device does this (it should come before any stream
+// capture); later calls whose stream is not capturing look it up again, so a
+// device reset (which gives the array a new address) leaves no stale pointer.
+static void *noalloc_scratch_address(cudaStream_t s) {
   int dev = 0;
   RCHOL_CUDA(cudaGetDevice(&dev));
-  RCHOL_CHECK_ARG(dev >= 0 && dev < 128, "device ordinal out of range");
+  RCHOL_CHECK_ARG(dev >= 0 && dev < kMaxDevices, "device ordinal out of range");
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    (void)cudaGetLastError();  // e.g. the legacy stream while another stream captures
+    cs = cudaStreamCaptureStatusActive;
+  }
   std::lock_guard<std::mutex> guard(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
+  if (!g_noalloc_ptr[dev] || cs == cudaStreamCaptureStatusNone) {
     void *p = nullptr;
     RCHOL_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
     g_noalloc_ptr[dev] = p;
@@ -1453,7 +1473,7 @@ void precond_noalloc(const rchol_factor_s &F, const double *r, double *z, cudaSt
                                        " bytes of scratch; the allocation-free entry point has " +
                                        std::to_string(kNoAllocScratchBytes) + " (n <= " +
                                        std::to_string(kNoAllocScratchBytes / (2 * vsz)) + " for this precision)");
-  unsigned char *base = static_cast<unsigned char *>(noalloc_scratch_address());
+  unsigned char *base = static_cast<unsigned char *>(noalloc_scratch_address(s));
   const SolvePlan &P = *F.plan;
   if (fp32) {
     float *acc = reinterpret_cast<float *>(base);

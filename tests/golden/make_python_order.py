@@ -25,7 +25,7 @@ import scipy.sparse as sp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference/python/rchol_lap"
+REF = os.path.join(os.environ.get("RCHOL_REFERENCE_DIR", "/root/reference"), "python", "rchol_lap")
 OUT = os.path.join(ROOT, "oracle", "_ref", "pyref")
 CASES = [(8, 2), (10, 4), (12, 8), (16, 16), (20, 32)]
 
