@@ -11,19 +11,21 @@ namespace rchol {
 
 // Block stream of one direction (forward with L = G, backward with U = G^T).
 //
-// The rows of every tree node are cut into pieces that fit in shared memory
-// (pieces of one node are solved one after the other) and every piece into
-// blocks of 32 consecutive rows.  A piece's entries are
+// The rows of every tree node are cut into pieces (pieces of one node are
+// solved one after another) and every piece into blocks of 32 consecutive
+// rows.  A piece's entries are
 //   * external (columns outside the piece, already solved): a CSR over rows,
-//     ext_rp / ext_ci / ext_v, consumed by the prologue;
+//     ext_rp / ext_ci / ext_v, summed by an all-SM kernel before the stage;
 //   * in an earlier block of the piece: kept sparse in the block's record;
 //   * inside the block: folded into the exact inverse of the block's 32x32
-//     triangle, stored packed by columns (528 values).
-// Two record formats exist (trsv.cu documents both): the warp format, where
-// one warp solves a piece and lane r sums row r's sparse entries, and the
-// team format, where a thread block solves a piece, its helper warps sum the
-// entries from blocks older than the previous one in balanced chunks, and
-// one warp adds the previous block's entries and applies the inverse.
+//     triangle.
+// Record formats (trsv.cu documents each): FMT_WARP, one warp per piece with
+// a window of solved values (depths with many nodes); FMT_PIPE, one thread
+// block per piece whose warps split a block's entries by distance (the few
+// long chains at the top of the tree); FMT_KTEAM, a thread block per piece
+// for 32 right-hand sides at once.
+enum { FMT_WARP = 0, FMT_PIPE = 1, FMT_KTEAM = 2 };
+
 struct NodeDesc {
   int64_t begin;    // first row of the piece
   int32_t rows;
@@ -31,7 +33,7 @@ struct NodeDesc {
   int64_t blk0;     // offsets of its blocks: blk_off[blk0 .. blk0 + nblocks]
   int32_t maxrec;   // largest block record (bytes)
   int32_t wide;     // column indices are u32 (piece larger than 65535 rows)
-  int32_t maxchunk; // team format: most chunks of one block
+  int32_t maxchunk; // pipeline / k-team formats: most chunks of one block
   int32_t pad_;
 };
 
@@ -39,12 +41,13 @@ struct StreamDir {
   std::vector<int> stage_ptr;        // pieces of stage s: [stage_ptr[s], stage_ptr[s+1])
   std::vector<int> stage_rows;       // largest piece of the stage (rows)
   std::vector<int> stage_maxrec;     // largest block record of the stage (bytes)
-  std::vector<int64_t> stage_row_ptr;  // rows of split stages: srows[stage_row_ptr[s] ..]
-  std::vector<int> stage_team;       // 1: team format (a thread block per piece)
-  std::vector<int> stage_warps;      // team format: warps of the stage's teams
-  std::vector<int> stage_chunks;     // team format: most chunks of one block in the stage
-  std::vector<int> stage_ext_lanes;  // lanes per row of the external prologue (1, 4, 8 or 32)
-  int team_warps = 8;                // warps of a team (1 solver + helpers)
+  std::vector<int64_t> stage_row_ptr;  // rows of the stages: srows[stage_row_ptr[s] ..]
+  std::vector<int> stage_fmt;        // FMT_WARP, FMT_PIPE or FMT_KTEAM
+  std::vector<int> stage_warps;      // pipeline / k-team: warps of the stage's teams
+  std::vector<int> stage_chunks;     // pipeline / k-team: most chunks of one block in the stage
+  std::vector<int> stage_window;     // warp format: rows of the window of solved values (a power of two)
+  std::vector<int> stage_ext;        // 1: the stage has external entries (else it reads the rhs directly)
+  std::vector<int> stage_ext_lanes;  // lanes per row of the external sums (1, 4, 8 or 32)
   DevBuf<int32_t> srows;
   DevBuf<NodeDesc> nodes;
   DevBuf<int64_t> ext_rp;

@@ -398,7 +398,6 @@ void finish_factor(rchol_factor_s &F, cudaStream_t s) {
 }
 
 void build_plan(rchol_factor_s &F, cudaStream_t s) {
-  const int64_t n = F.n, nnz = F.nnz;
   auto P = new SolvePlan();
   try {
     build_streams(F, *P, s);

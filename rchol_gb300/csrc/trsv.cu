@@ -1,4 +1,4 @@
-// Dense-block triangular solves with G (forward) and G^T (backward).
+// Block triangular solves with G (forward) and G^T (backward).
 //
 // Replaces the two MKL trsv calls of c++/util/pcg.cpp:141-159.
 //
@@ -11,22 +11,23 @@
 // step then retires 32 rows instead of one level.
 //
 // Schedule.  The tree is processed one depth at a time (leaves first for the
-// forward solve, root first for the backward one).  A node larger than shared
+// forward solve, root first for the backward one); a node larger than shared
 // memory is cut into pieces solved one after another.  Per stage:
 //   ext_kernel    acc_i = rhs_i - sum of row i's entries outside its piece
-//                 (columns already solved), all SMs; 1, 4, 8 or 32 lanes per
-//                 row (ext_lanes_kernel) by the stage's mean row length.
-//   team_kernel   one thread block per piece (default): the piece's unknowns
-//                 live in shared memory, block records stream in through a
-//                 cp.async ring; warp 0 solves block k (near entries from the
-//                 previous block by shuffles, then the dense inverse) while
-//                 the helper warps sum the far entries of block k + 1:
-//                   t_r = acc_r - sum_{earlier blocks} G_rj x_j   (sparse)
-//                   x_r = sum_c (T^-1)_{rc} t_c                   (dense, 32 shuffles)
-//   block_kernel  one warp per piece, the same arithmetic without helpers
-//                 (depths whose blocks are too dense for the team ring).
-// Values are FP32 or FP64 as the factor is stored; the block inverses are
-// computed in FP64 on the host and rounded to the stored precision.
+//                 (columns already solved), all SMs; skipped for stages
+//                 without such entries (the forward leaves), which read the
+//                 right-hand side directly.
+//   w2_kernel     depths with many nodes: one warp per piece, many pieces per
+//                 SM; lane r sums row r's entries in earlier blocks from a
+//                 window of recently solved values, then x = T^-1 t.
+//   pipe_kernel   the top of the tree: one thread block per piece whose
+//                 warps split each block's entries by distance, so that the
+//                 step on the chain (the solver warp) only adds the previous
+//                 block's entries and applies the inverse.
+// Records stream into shared memory with bulk copies (cp.async.bulk +
+// mbarrier); the block inverses are computed in FP64 on the host and rounded
+// to the stored precision.  32 right-hand sides at once use the k-team format
+// (team_k_kernel).
 
 #include <algorithm>
 #include <cmath>
@@ -85,87 +86,6 @@ void invert_block(double T[BS][BS], bool upper, double X[BS][BS]) {
         X[i][j] = -s / T[i][i];
       }
     }
-  }
-}
-
-void build_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, const std::vector<double> &v,
-                 int64_t b, int64_t e, bool upper, size_t vsz, PieceBuild &P) {
-  const int64_t R = e - b, nb = (R + BS - 1) / BS;
-  const size_t csz = R > 65535 ? 4 : 2;
-  P.offs.assign(1, 0);
-  P.bytes.clear();
-  double T[BS][BS], X[BS][BS];
-  std::vector<uint32_t> cols[BS];
-  std::vector<double> vals[BS];
-  for (int64_t s = 0; s < nb; ++s) {
-    const int64_t bi = upper ? nb - 1 - s : s;
-    const int64_t row0 = bi * BS;
-    const int nr = (int)std::min<int64_t>(BS, R - row0);
-    for (int r = 0; r < BS; ++r) {
-      for (int c = 0; c < BS; ++c) T[r][c] = 0.0;
-      T[r][r] = 1.0;
-      cols[r].clear();
-      vals[r].clear();
-    }
-    uint32_t nent = 0;
-    for (int r = 0; r < nr; ++r) {
-      const int64_t i = b + row0 + r;
-      for (int64_t q = rp[i]; q < rp[i + 1]; ++q) {
-        const int64_t c = ci[q];
-        if (c < b || c >= e) continue;  // external
-        const int64_t lc = c - b;
-        if (lc >= row0 && lc < row0 + nr) {
-          T[r][lc - row0] = v[q];  // inside the block (diagonal included)
-        } else {
-          cols[r].push_back((uint32_t)lc);
-          vals[r].push_back(v[q]);
-          ++nent;
-        }
-      }
-    }
-    invert_block(T, upper, X);
-    // record layout
-    const size_t o_off = 16, o_col = o_off + al16(4 * (BS + 1)), o_val = o_col + al16(csz * nent),
-                 o_min = o_val + al16(vsz * nent), len = o_min + al16(vsz * TRI);
-    const size_t base = P.bytes.size();
-    P.bytes.resize(base + len, 0);
-    unsigned char *p = P.bytes.data() + base;
-    uint32_t hdr[4] = {(uint32_t)nr, nent, (uint32_t)row0, (uint32_t)csz};
-    std::memcpy(p, hdr, 16);
-    uint32_t off[BS + 1];
-    off[0] = 0;
-    for (int r = 0; r < BS; ++r) off[r + 1] = off[r] + (uint32_t)cols[r].size();
-    std::memcpy(p + o_off, off, 4 * (BS + 1));
-    size_t w = 0;
-    for (int r = 0; r < BS; ++r)
-      for (size_t t = 0; t < cols[r].size(); ++t, ++w) {
-        if (csz == 2) {
-          uint16_t c16 = (uint16_t)cols[r][t];
-          std::memcpy(p + o_col + 2 * w, &c16, 2);
-        } else {
-          std::memcpy(p + o_col + 4 * w, &cols[r][t], 4);
-        }
-        if (vsz == 8) std::memcpy(p + o_val + 8 * w, &vals[r][t], 8);
-        else {
-          float f = (float)vals[r][t];
-          std::memcpy(p + o_val + 4 * w, &f, 4);
-        }
-      }
-    for (int c = 0; c < BS; ++c) {
-      const int r_lo = upper ? 0 : c, r_hi = upper ? c : BS - 1;
-      for (int r = r_lo; r <= r_hi; ++r) {
-        const double m = (r < nr && c < nr) ? X[r][c] : 0.0;
-        const size_t at = (size_t)tri_col_off(c, upper) + (size_t)(r - r_lo);
-        if (vsz == 8) std::memcpy(p + o_min + 8 * at, &m, 8);
-        else {
-          float f = (float)m;
-          std::memcpy(p + o_min + 4 * at, &f, 4);
-        }
-      }
-    }
-    P.offs.push_back((int64_t)P.bytes.size());
-    P.maxrec = std::max<int32_t>(P.maxrec, (int32_t)len);
-    P.sparse += nent;
   }
 }
 
@@ -439,142 +359,6 @@ __global__ void __launch_bounds__(256) ext_kernel(const int32_t *__restrict__ ro
   acc[i] = (VT)in[i] - (s0 + s1);
 }
 
-template <typename VT>
-struct BlockArgs {
-  const NodeDesc *nodes;
-  int node0, node1;     // pieces of this stage
-  int wpb;              // warps (pieces) per thread block
-  int bufbytes;         // per-buffer bytes (16-aligned)
-  int nbuf;             // block records in flight per warp (ring of buffers), 2..6
-  int per_warp;         // shared-memory bytes per warp
-  bool upper;           // backward solve: upper-triangular block inverses
-  const unsigned char *blocks;
-  const int64_t *blk_off;
-  const VT *acc;
-};
-
-template <typename VT, typename OutT, bool UPPER>
-__global__ void __launch_bounds__(128) block_kernel(BlockArgs<VT> a, OutT *out) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int piece = a.node0 + blockIdx.x * a.wpb + w;
-  if (piece >= a.node1) return;  // the whole warp leaves
-  const NodeDesc nd = a.nodes[piece];
-  unsigned char *base = smem + (size_t)w * a.per_warp;
-  const int nbuf = a.nbuf;
-  VT *xs = reinterpret_cast<VT *>(base + (size_t)nbuf * a.bufbytes);
-  const unsigned char *src = a.blocks;
-  const int64_t *boff = a.blk_off + nd.blk0;
-
-  // ring of nbuf block buffers; block k lives in slot k % nbuf
-  auto load = [&](int k) {
-    unsigned char *dst = base + (size_t)(k % nbuf) * a.bufbytes;
-    const int64_t o0 = boff[k];
-    int64_t len = boff[k + 1] - o0;
-#ifdef RCHOL_DEVICE_CHECKS
-    if (len < 0 || len > a.bufbytes || (o0 & 15)) {
-      if (lane == 0) dbg_report("block record length", len, a.bufbytes);
-      len = 0;
-    }
-#endif
-    for (int64_t o = lane * 16; o < len; o += 32 * 16) cp_async16(dst + o, src + o0 + o);
-    cp_async_commit();
-  };
-#ifdef RCHOL_DEVICE_CHECKS
-  if ((int64_t)nbuf * a.bufbytes + (int64_t)nd.rows * (int64_t)sizeof(VT) > a.per_warp ||
-      nd.begin < 0 || nd.begin + nd.rows > dbg_n) {
-    if (lane == 0) dbg_report("piece layout (rows)", nd.rows, a.per_warp);
-    return;
-  }
-#endif
-  for (int k = 0; k < nbuf - 1 && k < nd.nblocks; ++k) load(k);
-  for (int r = lane; r < nd.rows; r += 32) xs[r] = a.acc[nd.begin + r];
-  __syncwarp();
-
-  for (int k = 0; k < nd.nblocks; ++k) {
-    // refill the slot block k-1 used (finished last step), then wait for block
-    // k; the groups committed after block k's may stay in flight
-    if (k + nbuf - 1 < nd.nblocks) load(k + nbuf - 1);
-    const int after = min(nbuf - 1, nd.nblocks - 1 - k);
-    switch (after) {
-      case 0: cp_async_wait<0>(); break;
-      case 1: cp_async_wait<1>(); break;
-      case 2: cp_async_wait<2>(); break;
-      case 3: cp_async_wait<3>(); break;
-      case 4: cp_async_wait<4>(); break;
-      default: cp_async_wait<5>(); break;
-    }
-    __syncwarp();
-    const unsigned char *p = base + (size_t)(k % nbuf) * a.bufbytes;
-    const uint32_t *hdr = reinterpret_cast<const uint32_t *>(p);
-    const uint32_t nr = hdr[0], nent = hdr[1], row0 = hdr[2], csz = hdr[3];
-    const uint32_t *eoff = reinterpret_cast<const uint32_t *>(p + 16);
-    const size_t o_col = 16 + al16(4 * (BS + 1));
-    const size_t o_val = o_col + al16((size_t)csz * nent);
-    const size_t o_min = o_val + al16(sizeof(VT) * nent);
-    const VT *val = reinterpret_cast<const VT *>(p + o_val);
-    const VT *minv = reinterpret_cast<const VT *>(p + o_min);
-#ifdef RCHOL_DEVICE_CHECKS
-    if (nr > (uint32_t)BS || (int64_t)row0 + nr > nd.rows || (csz != 2 && csz != 4) || eoff[BS] != nent ||
-        (int64_t)(o_min + sizeof(VT) * TRI) > a.bufbytes) {
-      if (lane == 0) dbg_report("block header (row0)", row0, nd.rows);
-      return;
-    }
-    bool badc = false;
-    for (uint32_t e = eoff[lane]; e < eoff[lane + 1]; ++e) {
-      const uint32_t cc = csz == 2 ? reinterpret_cast<const uint16_t *>(p + o_col)[e]
-                                   : reinterpret_cast<const uint32_t *>(p + o_col)[e];
-      if (cc >= (uint32_t)nd.rows) {
-        dbg_report("block column", cc, nd.rows);
-        badc = true;
-      }
-    }
-    if (__any_sync(0xffffffffu, badc)) return;
-#endif
-    VT t = 0;
-    if (lane < (int)nr) {
-      VT s0 = 0, s1 = 0;
-      uint32_t e = eoff[lane];
-      const uint32_t e1 = eoff[lane + 1];
-      if (csz == 2) {
-        const uint16_t *col = reinterpret_cast<const uint16_t *>(p + o_col);
-        for (; e + 1 < e1; e += 2) {
-          s0 += val[e] * xs[col[e]];
-          s1 += val[e + 1] * xs[col[e + 1]];
-        }
-        if (e < e1) s0 += val[e] * xs[col[e]];
-      } else {
-        const uint32_t *col = reinterpret_cast<const uint32_t *>(p + o_col);
-        for (; e + 1 < e1; e += 2) {
-          s0 += val[e] * xs[col[e]];
-          s1 += val[e + 1] * xs[col[e + 1]];
-        }
-        if (e < e1) s0 += val[e] * xs[col[e]];
-      }
-      t = xs[row0 + lane] - (s0 + s1);
-    }
-    // x_lane = sum_c Minv[lane][c] t_c over the stored triangle
-    VT c0 = 0, c1 = 0, c2 = 0, c3 = 0;
-    auto term = [&](int c) -> VT {
-      const VT tc = __shfl_sync(0xffffffffu, t, c);
-      const bool in = UPPER ? (lane <= c) : (lane >= c);
-      const int at = tri_col_off(c, UPPER) + (UPPER ? lane : lane - c);
-      return in ? minv[at] * tc : VT(0);
-    };
-#pragma unroll
-    for (int c = 0; c < BS; c += 4) {
-      c0 += term(c + 0);
-      c1 += term(c + 1);
-      c2 += term(c + 2);
-      c3 += term(c + 3);
-    }
-    if (lane < (int)nr) xs[row0 + lane] = (c0 + c1) + (c2 + c3);
-    __syncwarp();
-  }
-  __syncwarp();
-  for (int r = lane; r < nd.rows; r += 32) out[nd.begin + r] = (OutT)xs[r];
-}
-
 // acc_i = rhs_i - sum over row i's entries outside its piece, LANES lanes per
 // row (long external rows at the top of the tree); fixed summation order.
 template <typename VT, typename InT, typename OutT, int LANES>
@@ -639,145 +423,6 @@ __device__ __forceinline__ TeamHdr read_hdr(const unsigned char *p) {
   const uint4 *q = reinterpret_cast<const uint4 *>(p);
   const uint4 a = q[0], b = q[1], c = q[2], d = q[3];
   return TeamHdr{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
-}
-
-// Sum of chunk c: clen entries interleaved with stride nchunk.
-template <typename VT, typename CT>
-__device__ __forceinline__ VT chunk_sum(const CT *col, const VT *val, const VT *x, uint32_t c, uint32_t nchunk,
-                                        uint32_t clen) {
-  VT s0 = 0, s1 = 0;
-  uint32_t j = 0, at = c;
-  for (; j + 1 < clen; j += 2, at += 2 * nchunk) {
-    s0 += val[at] * x[col[at]];
-    s1 += val[at + nchunk] * x[col[at + nchunk]];
-  }
-  if (j < clen) s0 += val[at] * x[col[at]];
-  return s0 + s1;
-}
-
-// Named barrier of the helper warps only (the solver does not take part).
-__device__ __forceinline__ void helpers_sync(int nthreads) {
-  asm volatile("bar.sync 1, %0;\n" ::"r"(nthreads) : "memory");
-}
-
-// One thread block per piece.  Per step k (one __syncthreads):
-//   warp 0   t = u_k - near_k . x_{k-1} (shuffles of the previous block's
-//            solution, kept in registers), x_k = T_k^-1 t (shuffles);
-//   helpers  chunk sums of block k+1 (columns solved before block k), then
-//            warp 1 folds them per row into u_{k+1} = acc - far; all helper
-//            threads stream record k+RING-1 into the ring.
-// The solver's chain per step is therefore only shuffles and FMAs; every
-// load it issues is independent of the previous block.
-template <typename VT, typename OutT, bool UPPER>
-__global__ void __launch_bounds__(256, 2) team_kernel(TeamArgs<VT> a, OutT *out) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int ht = tid - 32, TH = (int)blockDim.x - 32;  // helper thread index / count
-  unsigned char *ring = smem;
-  const int RING = a.ring;
-  VT *part = reinterpret_cast<VT *>(smem + (size_t)RING * a.bufbytes);  // chunk sums of the next block
-  VT *ubuf = reinterpret_cast<VT *>(reinterpret_cast<unsigned char *>(part) + al16((size_t)a.maxchunk * sizeof(VT)));
-  VT *xs = ubuf + 2 * BS;  // u of blocks k and k+1 (parity), then the piece's unknowns
-  const unsigned char *src = a.blocks;
-  const int64_t *boff = a.blk_off + nd.blk0;
-  const int nb = nd.nblocks;
-
-  auto load = [&](int k, int slot) {  // helpers only; one commit group per record (empty past the end)
-    if (k < nb) {
-      unsigned char *dst = ring + (size_t)slot * a.bufbytes;
-      const int64_t o0 = boff[k], len = boff[k + 1] - o0;
-      for (int64_t o = (int64_t)ht * 16; o < len; o += (int64_t)TH * 16) cp_async16(dst + o, src + o0 + o);
-    }
-    cp_async_commit();
-  };
-  for (int r = tid; r < nd.rows; r += blockDim.x) xs[r] = a.acc[nd.begin + r];
-  if (warp > 0) {
-    for (int k = 0; k < RING - 1; ++k) load(k, k);
-    cp_async_wait_upto(RING - 3);  // records 0 and 1 are in
-  }
-  __syncthreads();
-
-  VT xprev = 0;  // solver: x of the previous block, lane c = its row c
-  int slot = 0;  // ring slot of record k
-  for (int k = 0; k < nb; ++k) {
-    const int next = slot + 1 == RING ? 0 : slot + 1;
-    if (warp == 0) {
-      const unsigned char *p = ring + (size_t)slot * a.bufbytes;
-      const TeamHdr h = read_hdr(p);
-      const VT *minv = reinterpret_cast<const VT *>(p + h.o_min);
-      // the lane's row of the inverse (zero outside the triangle)
-      VT m[BS];
-#pragma unroll
-      for (int c = 0; c < BS; ++c) {
-        const bool in = UPPER ? (lane <= c) : (lane >= c);
-        m[c] = minv[in ? tri_col_off(c, UPPER) + (UPPER ? lane : lane - c) : 0];
-        m[c] = in ? m[c] : VT(0);
-      }
-      const bool row = lane < (int)h.nr;
-      // u = acc - far (block 0 has no far entries)
-      const VT u = !row ? VT(0) : k == 0 ? xs[h.row0 + lane] : ubuf[(k & 1) * BS + lane];
-      const uint16_t *noff = reinterpret_cast<const uint16_t *>(p + h.o_noff);
-      const unsigned char *ncol = p + h.o_ncol;
-      const VT *nval = reinterpret_cast<const VT *>(p + h.o_nval);
-      const uint32_t e0 = noff[lane], cnt = row ? noff[lane + 1] - e0 : 0;
-      VT s0 = 0, s1 = 0;
-      uint32_t j = 0;
-      for (; j + 1 < h.nmax; j += 2) {  // uniform trip count: every lane takes part in the shuffles
-        const bool ok0 = j < cnt, ok1 = j + 1 < cnt;
-        const int c0 = ok0 ? ncol[e0 + j] : 0, c1 = ok1 ? ncol[e0 + j + 1] : 0;
-        const VT v0 = ok0 ? nval[e0 + j] : VT(0), v1 = ok1 ? nval[e0 + j + 1] : VT(0);
-        s0 += v0 * __shfl_sync(0xffffffffu, xprev, c0);
-        s1 += v1 * __shfl_sync(0xffffffffu, xprev, c1);
-      }
-      if (j < h.nmax) {
-        const bool ok0 = j < cnt;
-        const int c0 = ok0 ? ncol[e0 + j] : 0;
-        const VT v0 = ok0 ? nval[e0 + j] : VT(0);
-        s0 += v0 * __shfl_sync(0xffffffffu, xprev, c0);
-      }
-      const VT t = u - (s0 + s1);
-      VT d0 = 0, d1 = 0, d2 = 0, d3 = 0;
-#pragma unroll
-      for (int c = 0; c < BS; c += 4) {
-        d0 += m[c + 0] * __shfl_sync(0xffffffffu, t, c + 0);
-        d1 += m[c + 1] * __shfl_sync(0xffffffffu, t, c + 1);
-        d2 += m[c + 2] * __shfl_sync(0xffffffffu, t, c + 2);
-        d3 += m[c + 3] * __shfl_sync(0xffffffffu, t, c + 3);
-      }
-      const VT x = (d0 + d1) + (d2 + d3);
-      if (row) xs[h.row0 + lane] = x;
-      xprev = x;
-    } else {
-      if (k + 1 < nb) {  // block k+1: far sums (columns solved before block k), then u per row
-        const unsigned char *p = ring + (size_t)next * a.bufbytes;
-        const TeamHdr h = read_hdr(p);
-        const VT *fval = reinterpret_cast<const VT *>(p + h.o_fval);
-        for (int c = ht; c < (int)h.nchunk; c += TH)
-          part[c] = h.csz == 2 ? chunk_sum(reinterpret_cast<const uint16_t *>(p + h.o_fcol), fval, xs, c, h.nchunk, h.clen)
-                               : chunk_sum(reinterpret_cast<const uint32_t *>(p + h.o_fcol), fval, xs, c, h.nchunk, h.clen);
-        helpers_sync(TH);
-        if (ht < BS) {
-          const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h.o_crow);
-          VT f0 = 0, f1 = 0;
-          uint32_t c = crow[ht];
-          const uint32_t c1 = crow[ht + 1];
-          for (; c + 1 < c1; c += 2) {
-            f0 += part[c];
-            f1 += part[c + 1];
-          }
-          if (c < c1) f0 += part[c];
-          ubuf[((k + 1) & 1) * BS + ht] = ht < (int)h.nr ? xs[h.row0 + ht] - (f0 + f1) : VT(0);
-        }
-      }
-      // record k+RING-1 goes into the slot of record k-1, retired last step
-      load(k + RING - 1, slot == 0 ? RING - 1 : slot - 1);
-      cp_async_wait_upto(RING - 3);  // records up to k+2 are in
-    }
-    slot = next;
-    __syncthreads();
-  }
-  for (int r = tid; r < nd.rows; r += blockDim.x) out[nd.begin + r] = (OutT)xs[r];
 }
 
 // ---- several right-hand sides -----------------------------------------------------
@@ -924,6 +569,756 @@ __global__ void __launch_bounds__(256, 1) team_k_kernel(TeamArgs<VT> a, OutT *ou
   }
 }
 
+// ---- single right-hand side: the packed block inverse ---------------------------------
+//
+// Row r of a block's inverse is stored by quads of 4 values: columns 0..r of
+// a lower (forward) inverse in quads 0..r/4, columns r..31 of an upper
+// (backward) one in quads r/4..7, zero-padded inside the end quads.  The
+// lane that owns row r loads its row with at most eight 16-byte reads and
+// multiplies it with the block's right-hand side t, which every lane reads
+// from shared memory as the same eight quads (broadcast reads).
+constexpr int TQ = 144;  // quads of one packed inverse (576 values)
+
+__host__ __device__ inline int tq_lo(int r, bool upper) { return upper ? (r >> 2) : 0; }
+__host__ __device__ inline int tq_hi(int r, bool upper) { return upper ? 7 : (r >> 2); }
+// first quad of row r: sum over earlier rows of their quad counts
+__host__ __device__ inline int tq_off(int r, bool upper) {
+  const int q = r >> 2, m = r & 3;
+  return upper ? 8 * r - 2 * q * (q - 1) - m * q : 2 * q * (q + 1) + m * (q + 1);
+}
+
+inline void put_val(unsigned char *p, size_t vsz, size_t idx, double x) {
+  if (vsz == 8) std::memcpy(p + 8 * idx, &x, 8);
+  else {
+    const float f = (float)x;
+    std::memcpy(p + 4 * idx, &f, 4);
+  }
+}
+
+// X: the inverse of the block's triangle (rows/columns >= nr unused).
+void put_tinv(unsigned char *p, size_t vsz, const double X[BS][BS], int nr, bool upper) {
+  for (int r = 0; r < BS; ++r)
+    for (int q = tq_lo(r, upper); q <= tq_hi(r, upper); ++q)
+      for (int j = 0; j < 4; ++j) {
+        const int c = 4 * q + j;
+        const bool in = upper ? c >= r : c <= r;
+        put_val(p, vsz, 4 * (size_t)(tq_off(r, upper) + q - tq_lo(r, upper)) + j,
+                (in && r < nr && c < nr) ? X[r][c] : 0.0);
+      }
+}
+
+// ---- warp format: one warp per piece -------------------------------------------------
+//
+// Lane r owns row r of a block: it sums the row's entries in earlier blocks
+// of the piece (already solved) and applies the inverse.  The piece's solved
+// values live in a window of W rows of shared memory (row i at i mod W): the
+// planner picks W above the longest distance between a row and the columns
+// it reads, so nodes of thousands of rows whose entries stay near the
+// diagonal (the leaves) need only a few KB.  Record (16-byte sections):
+//   u32 hdr[4]        nrows, row0, nent, col_bytes
+//   u16 eoff[33]      row r's entries [eoff[r], eoff[r+1])
+//   u16|u32 col[nent] piece-local columns
+//   VT  val[nent]
+//   VT  tinv[576]     packed inverse
+struct W2Layout {
+  size_t o_eoff, o_col, o_val, o_tinv, len;
+};
+
+__host__ __device__ inline W2Layout w2_layout(uint32_t nent, uint32_t csz, uint32_t vsz) {
+  W2Layout L;
+  L.o_eoff = 16;
+  L.o_col = 16 + al16(2 * (BS + 1));
+  L.o_val = L.o_col + al16((size_t)csz * nent);
+  L.o_tinv = L.o_val + al16((size_t)vsz * nent);
+  L.len = L.o_tinv + (size_t)vsz * 4 * TQ;
+  return L;
+}
+
+inline size_t w2_record_bound(size_t cnt, size_t vsz, size_t csz) {
+  return 16 + al16(2 * (BS + 1)) + al16(csz * cnt) + al16(vsz * cnt) + vsz * 4 * TQ;
+}
+
+// Records of one warp-format piece; `reach` returns the longest distance
+// (in rows) between a row and a column it reads inside the piece.
+void build_w2_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, const std::vector<double> &v,
+                    int64_t b, int64_t e, bool upper, size_t vsz, PieceBuild &P, int64_t &reach) {
+  const int64_t R = e - b, nb = (R + BS - 1) / BS;
+  const uint32_t csz = R > 65535 ? 4 : 2;
+  P.offs.assign(1, 0);
+  P.bytes.clear();
+  reach = 0;
+  double T[BS][BS], X[BS][BS];
+  std::vector<uint32_t> cols[BS];
+  std::vector<double> vals[BS];
+  for (int64_t s = 0; s < nb; ++s) {
+    const int64_t bi = upper ? nb - 1 - s : s;
+    const int64_t row0 = bi * BS;
+    const int nr = (int)std::min<int64_t>(BS, R - row0);
+    for (int r = 0; r < BS; ++r) {
+      for (int c = 0; c < BS; ++c) T[r][c] = 0.0;
+      T[r][r] = 1.0;
+      cols[r].clear();
+      vals[r].clear();
+    }
+    uint32_t nent = 0;
+    for (int r = 0; r < nr; ++r) {
+      const int64_t i = b + row0 + r;
+      for (int64_t q = rp[i]; q < rp[i + 1]; ++q) {
+        const int64_t c = ci[q];
+        if (c < b || c >= e) continue;  // external
+        const int64_t lc = c - b;
+        reach = std::max<int64_t>(reach, std::abs(row0 + r - lc));
+        if (lc >= row0 && lc < row0 + nr) {
+          T[r][lc - row0] = v[q];
+        } else {
+          cols[r].push_back((uint32_t)lc);
+          vals[r].push_back(v[q]);
+          ++nent;
+        }
+      }
+    }
+    if (nent > 65535) throw Error(RCHOL_ERR_INTERNAL, "a 32-row block has too many entries for the warp format");
+    invert_block(T, upper, X);
+    const W2Layout L = w2_layout(nent, csz, (uint32_t)vsz);
+    const size_t base = P.bytes.size();
+    P.bytes.resize(base + L.len, 0);
+    unsigned char *p = P.bytes.data() + base;
+    const uint32_t hdr[4] = {(uint32_t)nr, (uint32_t)row0, nent, csz};
+    std::memcpy(p, hdr, 16);
+    uint16_t eoff[BS + 1];
+    eoff[0] = 0;
+    size_t w = 0;
+    for (int r = 0; r < BS; ++r) {
+      for (size_t t = 0; t < cols[r].size(); ++t, ++w) {
+        if (csz == 2) {
+          const uint16_t c16 = (uint16_t)cols[r][t];
+          std::memcpy(p + L.o_col + 2 * w, &c16, 2);
+        } else {
+          std::memcpy(p + L.o_col + 4 * w, &cols[r][t], 4);
+        }
+        put_val(p + L.o_val, vsz, w, vals[r][t]);
+      }
+      eoff[r + 1] = (uint16_t)w;
+    }
+    std::memcpy(p + L.o_eoff, eoff, sizeof(eoff));
+    put_tinv(p + L.o_tinv, vsz, X, nr, upper);
+    P.offs.push_back((int64_t)P.bytes.size());
+    P.maxrec = std::max<int32_t>(P.maxrec, (int32_t)L.len);
+    P.sparse += nent;
+  }
+}
+
+// ---- pipeline format: one thread block per piece --------------------------------------
+//
+// For the few long chains at the top of the tree.  Block k's entries in
+// earlier blocks of the piece are split by distance so that each step of the
+// chain carries as little as possible:
+//   distance 1 (block k-1) the solver warp, with the inverse: x_k = T^-1 t,
+//                          t = u_k - N1 x_{k-1};
+//   distance 2 (block k-2) the reducer warp, one step ahead:
+//                          u_k = acc_k - sum of chunk sums - N2 x_{k-2};
+//   distance >= 3          the gatherer warps, two steps ahead: chunk sums
+//                          over columns solved before block k-2.
+// Record (16-byte sections):
+//   u32 hdr[16]   nrows, row0, prow0, pprow0, n1, n2, nchunk, clen, col_bytes,
+//                 o_n1c, o_n1v, o_n2c, o_n2v, o_crow, o_fc, o_fv
+//   VT  tinv[576]                       packed inverse (at byte 64)
+//   u8  n1c[n1][32];  VT n1v[n1][32]    slot-major: entry j of row r at j*32 + r,
+//   u8  n2c[n2][32];  VT n2v[n2][32]    column within block k-1 / k-2 (padding 0, 0)
+//   u16 crow[33]                        row r's chunks [crow[r], crow[r+1])
+//   u16|u32 fc[clen][nchunk]; VT fv[..] entry j of chunk c at j*nchunk + c
+struct PipeLayout {
+  size_t o_n1c, o_n1v, o_n2c, o_n2v, o_crow, o_fc, o_fv, len;
+};
+
+__host__ __device__ inline PipeLayout pipe_layout(uint32_t n1, uint32_t n2, uint32_t nchunk, uint32_t clen,
+                                                  uint32_t csz, uint32_t vsz) {
+  PipeLayout L;
+  size_t o = 64 + (size_t)vsz * 4 * TQ;
+  L.o_n1c = o;
+  o += al16((size_t)BS * n1);
+  L.o_n1v = o;
+  o += al16((size_t)vsz * BS * n1);
+  L.o_n2c = o;
+  o += al16((size_t)BS * n2);
+  L.o_n2v = o;
+  o += al16((size_t)vsz * BS * n2);
+  L.o_crow = o;
+  o += al16(2 * (BS + 1));
+  L.o_fc = o;
+  o += al16((size_t)csz * nchunk * clen);
+  L.o_fv = o;
+  o += al16((size_t)vsz * nchunk * clen);
+  L.len = o;
+  return L;
+}
+
+// Upper bound of a pipeline record whose block has `cnt` entries in earlier
+// blocks of its piece, for `gthreads` gatherer threads.
+inline size_t pipe_record_bound(size_t cnt, size_t gthreads, size_t vsz, size_t csz) {
+  const size_t slots = gthreads > (size_t)BS ? gthreads - BS : 1;
+  const size_t clen = std::max<size_t>(1, (cnt + slots - 1) / slots);
+  const size_t padded = cnt + BS * clen;
+  const size_t nslot = (size_t)BS * std::min<size_t>(cnt, BS);
+  return 64 + vsz * 4 * TQ + 2 * (al16(nslot) + al16(vsz * nslot)) + al16(2 * (BS + 1)) + al16(csz * padded) +
+         al16(vsz * padded);
+}
+
+void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, const std::vector<double> &v,
+                      int64_t b, int64_t e, bool upper, size_t vsz, int gthreads, PieceBuild &P,
+                      int32_t &maxchunk) {
+  const int64_t R = e - b, nb = (R + BS - 1) / BS;
+  const uint32_t csz = R > 65535 ? 4 : 2;
+  P.offs.assign(1, 0);
+  P.bytes.clear();
+  maxchunk = 0;
+  double T[BS][BS], X[BS][BS];
+  std::vector<std::pair<uint32_t, double>> l1[BS], l2[BS], lf[BS];
+  for (int64_t s = 0; s < nb; ++s) {
+    const int64_t bi = upper ? nb - 1 - s : s;
+    const int64_t row0 = bi * BS;
+    const int nr = (int)std::min<int64_t>(BS, R - row0);
+    const int64_t b1 = upper ? bi + 1 : bi - 1, b2 = upper ? bi + 2 : bi - 2;  // blocks k-1, k-2
+    const bool has1 = s >= 1, has2 = s >= 2;
+    for (int r = 0; r < BS; ++r) {
+      for (int c = 0; c < BS; ++c) T[r][c] = 0.0;
+      T[r][r] = 1.0;
+      l1[r].clear();
+      l2[r].clear();
+      lf[r].clear();
+    }
+    uint32_t nfar = 0, n1 = 0, n2 = 0;
+    for (int r = 0; r < nr; ++r) {
+      const int64_t i = b + row0 + r;
+      for (int64_t q = rp[i]; q < rp[i + 1]; ++q) {
+        const int64_t c = ci[q];
+        if (c < b || c >= e) continue;  // external
+        const int64_t lc = c - b, cb = lc / BS;
+        if (cb == bi) T[r][lc - row0] = v[q];
+        else if (has1 && cb == b1) l1[r].push_back({(uint32_t)(lc - b1 * BS), v[q]});
+        else if (has2 && cb == b2) l2[r].push_back({(uint32_t)(lc - b2 * BS), v[q]});
+        else {
+          lf[r].push_back({(uint32_t)lc, v[q]});
+          ++nfar;
+        }
+      }
+      n1 = std::max<uint32_t>(n1, (uint32_t)l1[r].size());
+      n2 = std::max<uint32_t>(n2, (uint32_t)l2[r].size());
+    }
+    invert_block(T, upper, X);
+    // far entries in chunks of clen (a row's last chunk padded), one chunk
+    // per gatherer thread: every row adds at most one partial chunk
+    const int slots = std::max(1, gthreads - BS);
+    const uint32_t clen = std::max<uint32_t>(1, (nfar + slots - 1) / slots);
+    uint16_t crow[BS + 1];
+    crow[0] = 0;
+    uint32_t nchunk = 0;
+    for (int r = 0; r < BS; ++r) {
+      nchunk += ((uint32_t)lf[r].size() + clen - 1) / clen;
+      crow[r + 1] = (uint16_t)nchunk;
+    }
+    if (nchunk > (uint32_t)gthreads) throw Error(RCHOL_ERR_INTERNAL, "pipeline record: more chunks than gatherers");
+    maxchunk = std::max<int32_t>(maxchunk, (int32_t)nchunk);
+    const PipeLayout L = pipe_layout(n1, n2, nchunk, clen, csz, (uint32_t)vsz);
+    const size_t base = P.bytes.size();
+    P.bytes.resize(base + L.len, 0);
+    unsigned char *p = P.bytes.data() + base;
+    const int64_t prow0 = has1 ? b1 * BS : 0, pprow0 = has2 ? b2 * BS : 0;
+    const uint32_t hdr[16] = {(uint32_t)nr,       (uint32_t)row0,     (uint32_t)prow0,    (uint32_t)pprow0,
+                              n1,                 n2,                 nchunk,             clen,
+                              csz,                (uint32_t)L.o_n1c,  (uint32_t)L.o_n1v,  (uint32_t)L.o_n2c,
+                              (uint32_t)L.o_n2v,  (uint32_t)L.o_crow, (uint32_t)L.o_fc,   (uint32_t)L.o_fv};
+    std::memcpy(p, hdr, sizeof(hdr));
+    put_tinv(p + 64, vsz, X, nr, upper);
+    for (int r = 0; r < BS; ++r) {
+      for (size_t j = 0; j < l1[r].size(); ++j) {
+        p[L.o_n1c + j * BS + r] = (unsigned char)l1[r][j].first;
+        put_val(p + L.o_n1v, vsz, j * BS + r, l1[r][j].second);
+      }
+      for (size_t j = 0; j < l2[r].size(); ++j) {
+        p[L.o_n2c + j * BS + r] = (unsigned char)l2[r][j].first;
+        put_val(p + L.o_n2v, vsz, j * BS + r, l2[r][j].second);
+      }
+    }
+    std::memcpy(p + L.o_crow, crow, sizeof(crow));
+    // chunk c holds row r's far entries crow[r]*clen.. in column order; within
+    // each warp's 32 chunks the entries of one step are picked greedily so that
+    // the gathers of the solved values hit distinct shared-memory banks where
+    // possible (the chunk's sum does not depend on that order beyond
+    // rounding); padding entries (value 0) take a column of a free bank
+    std::vector<std::vector<std::pair<uint32_t, double>>> chunkl(nchunk);
+    for (int r = 0; r < BS; ++r)
+      for (size_t q = 0; q < lf[r].size(); ++q) chunkl[crow[r] + q / clen].push_back(lf[r][q]);
+    const uint32_t nbank = vsz == 4 ? 32 : 16;
+    for (uint32_t g0 = 0; g0 < nchunk; g0 += 32) {
+      const uint32_t g1 = std::min(nchunk, g0 + 32);
+      std::vector<std::vector<char>> taken(g1 - g0);
+      for (uint32_t c = g0; c < g1; ++c) taken[c - g0].assign(chunkl[c].size(), 0);
+      for (uint32_t j = 0; j < clen; ++j) {
+        std::vector<char> busy(nbank, 0);
+        std::vector<int> pick(g1 - g0, -1);
+        for (uint32_t c = g0; c < g1; ++c) {
+          const auto &lst = chunkl[c];
+          int first = -1;
+          for (size_t q = 0; q < lst.size(); ++q) {
+            if (taken[c - g0][q]) continue;
+            if (first < 0) first = (int)q;
+            if (!busy[lst[q].first % nbank]) {
+              pick[c - g0] = (int)q;
+              break;
+            }
+          }
+          if (pick[c - g0] < 0) pick[c - g0] = first;
+          if (pick[c - g0] >= 0) {
+            taken[c - g0][pick[c - g0]] = 1;
+            busy[lst[pick[c - g0]].first % nbank] = 1;
+          }
+        }
+        for (uint32_t c = g0; c < g1; ++c) {
+          uint32_t col;
+          double val;
+          if (pick[c - g0] >= 0) {
+            col = chunkl[c][pick[c - g0]].first;
+            val = chunkl[c][pick[c - g0]].second;
+          } else {  // padding
+            uint32_t bank = 0;
+            while (bank + 1 < nbank && (busy[bank] || bank >= R)) ++bank;
+            busy[bank] = 1;
+            col = bank < R ? bank : 0;
+            val = 0.0;
+          }
+          const size_t at = (size_t)j * nchunk + c;
+          if (csz == 2) {
+            const uint16_t c16 = (uint16_t)col;
+            std::memcpy(p + L.o_fc + 2 * at, &c16, 2);
+          } else {
+            std::memcpy(p + L.o_fc + 4 * at, &col, 4);
+          }
+          put_val(p + L.o_fv, vsz, at, val);
+        }
+      }
+    }
+    P.offs.push_back((int64_t)P.bytes.size());
+    P.maxrec = std::max<int32_t>(P.maxrec, (int32_t)L.len);
+    P.sparse += nfar;
+    for (int r = 0; r < BS; ++r) P.sparse += l1[r].size() + l2[r].size();
+  }
+}
+
+// ---- bulk copies into shared memory ----------------------------------------------------
+//
+// Records stream into a ring of shared-memory slots with cp.async.bulk (the
+// copy engine moves a whole record; no thread issues 16-byte pieces), one
+// mbarrier per slot counting the record's bytes.  Far-ahead records are
+// prefetched into L2.  Every wait is bounded: after kWaitLimit polls the
+// kernel records bit 0 in g_solve_status, stops issuing copies, waits
+// (bounded) for the ones in flight and finishes without using the data.
+
+constexpr uint32_t kWaitLimit = 1u << 22;
+__device__ unsigned int g_solve_status;  // bit 0: a bounded wait gave up
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// orders this thread's earlier shared-memory accesses before later async-proxy (bulk copy) ones
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ void prefetch_l2(const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for the phase of `parity` to complete; false after kWaitLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_test(bar, parity)) return true;
+  return false;
+}
+
+// Byte offsets of a piece's records, held by the 32 lanes of one warp: lane j
+// has boff[32c + j] (window A) and boff[32c + 32 + j] (window B); get(k) is a
+// warp-wide shuffle and valid for 32c <= k < 32c + 64.  advance(k) slides the
+// windows once k reaches 32c + 32, loading the next 32 offsets about 32
+// records before they are needed (offsets past the end read the last one).
+struct OffCache {
+  const int64_t *boff;
+  int last;  // index of the last offset (= number of records)
+  int c32;   // 32c
+  int64_t a, b;
+  __device__ void init(const int64_t *p, int nrec, int lane) {
+    boff = p;
+    last = nrec;
+    c32 = 0;
+    a = boff[min(lane, last)];
+    b = boff[min(32 + lane, last)];
+  }
+  __device__ __forceinline__ int64_t get(int k) const {
+    const int64_t va = __shfl_sync(0xffffffffu, a, k & 31), vb = __shfl_sync(0xffffffffu, b, k & 31);
+    return k < c32 + 32 ? va : vb;
+  }
+  __device__ __forceinline__ void advance(int k, int lane) {
+    if (k >= c32 + 32) {
+      c32 += 32;
+      a = b;
+      b = boff[min(c32 + 32 + lane, last)];
+    }
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ void ld_quad(const T *p, T (&o)[4]);
+template <>
+__device__ __forceinline__ void ld_quad<float>(const float *p, float (&o)[4]) {
+  const float4 v = *reinterpret_cast<const float4 *>(p);
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+  o[3] = v.w;
+}
+template <>
+__device__ __forceinline__ void ld_quad<double>(const double *p, double (&o)[4]) {
+  const double2 u = reinterpret_cast<const double2 *>(p)[0], w = reinterpret_cast<const double2 *>(p)[1];
+  o[0] = u.x;
+  o[1] = u.y;
+  o[2] = w.x;
+  o[3] = w.y;
+}
+
+// Row `lane` of a packed inverse into registers (zero outside the triangle).
+template <typename VT, bool UPPER>
+__device__ __forceinline__ void load_tinv_row(const VT *tinv, int lane, VT (&m)[BS]) {
+  const int lo = tq_lo(lane, UPPER), hi = tq_hi(lane, UPPER), off = tq_off(lane, UPPER);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    VT v[4] = {VT(0), VT(0), VT(0), VT(0)};
+    if (q >= lo && q <= hi) ld_quad(tinv + 4 * (off + q - lo), v);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) m[4 * q + j] = v[j];
+  }
+}
+
+// sum_c m[c] t[c] with t read from shared memory as eight broadcast quads
+template <typename VT>
+__device__ __forceinline__ VT apply_row(const VT (&m)[BS], const VT *tb) {
+  VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    VT t[4];
+    ld_quad(tb + 4 * q, t);
+    a0 = fma(m[4 * q + 0], t[0], a0);
+    a1 = fma(m[4 * q + 1], t[1], a1);
+    a2 = fma(m[4 * q + 2], t[2], a2);
+    a3 = fma(m[4 * q + 3], t[3], a3);
+  }
+  return (a0 + a1) + (a2 + a3);
+}
+
+template <typename VT, typename InT>
+__device__ __forceinline__ VT rhs_at(const VT *acc, const InT *in, int64_t i) {
+  return acc ? __ldg(acc + i) : (VT)__ldg(in + i);
+}
+
+template <typename VT>
+struct W2Args {
+  const NodeDesc *nodes;
+  int node0, node1;   // pieces of this stage
+  int wpb;            // warps (pieces) per thread block
+  int nbuf;           // ring slots per warp
+  int bufbytes;       // bytes of a slot (16-aligned)
+  int per_warp;       // shared-memory bytes per warp (16-aligned)
+  int pf;             // records prefetched into L2 ahead of use (0: none)
+  uint32_t wmask;     // window rows - 1 (a power of two)
+  const unsigned char *blocks;
+  const int64_t *blk_off;
+  const VT *acc;      // rhs minus external sums, or null: the stage reads `in`
+};
+
+// One warp per piece; per-warp shared memory: mbarriers, the broadcast
+// buffer of t, the record ring, the window of solved values.
+template <typename VT, typename InT, typename OutT, bool UPPER>
+__global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__restrict__ in, OutT *__restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int piece = a.node0 + blockIdx.x * a.wpb + w;
+  if (piece >= a.node1) return;  // the whole warp; no block-wide barrier follows
+  const NodeDesc nd = a.nodes[piece];
+  const int nb = nd.nblocks, NB = a.nbuf;
+  unsigned char *base = smem + (size_t)w * a.per_warp;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(base);
+  VT *tsh = reinterpret_cast<VT *>(base + al16(8 * (size_t)NB));
+  unsigned char *ring = reinterpret_cast<unsigned char *>(tsh + BS);
+  VT *xw = reinterpret_cast<VT *>(ring + (size_t)NB * a.bufbytes);
+  const uint32_t wmask = a.wmask;
+  OffCache oc;
+  oc.init(a.blk_off + nd.blk0, nb, lane);
+  if (lane == 0) {
+    for (int i = 0; i < NB; ++i) mbar_init(bar + i, 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  auto issue = [&](int k) {  // all lanes (offset shuffles); lane 0 copies record k into slot k % NB
+    const int64_t o0 = oc.get(k), o1 = oc.get(k + 1);
+    if (lane == 0) bulk_load(ring + (size_t)(k % NB) * a.bufbytes, a.blocks + o0, (uint32_t)(o1 - o0), bar + k % NB);
+  };
+  for (int k = 0; k < NB && k < nb; ++k) issue(k);
+  auto rhs = [&](int k) -> VT {  // right-hand side of row `lane` of block k
+    const int row = (UPPER ? nb - 1 - k : k) * BS + lane;
+    return (k < nb && row < nd.rows) ? rhs_at(a.acc, in, nd.begin + row) : VT(0);
+  };
+  VT q0 = rhs(0), q1 = rhs(1), q2 = rhs(2);
+  int k = 0;
+  bool ok = true;
+  for (; k < nb; ++k) {
+    const int slot = k % NB;
+    ok = __all_sync(0xffffffffu, mbar_wait(bar + slot, (uint32_t)(k / NB) & 1u));
+    if (!ok) break;
+    const unsigned char *p = ring + (size_t)slot * a.bufbytes;
+    const uint4 h = *reinterpret_cast<const uint4 *>(p);
+    const uint32_t nr = h.x, row0 = h.y, nent = h.z, csz = h.w;
+    const W2Layout L = w2_layout(nent, csz, sizeof(VT));
+    VT m[BS];
+    load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + L.o_tinv), lane, m);
+    const uint16_t *eoff = reinterpret_cast<const uint16_t *>(p + L.o_eoff);
+    const VT *val = reinterpret_cast<const VT *>(p + L.o_val);
+    uint32_t e = eoff[lane];
+    const uint32_t e1 = eoff[lane + 1];
+    VT s0 = 0, s1 = 0;
+    if (csz == 2) {
+      const uint16_t *col = reinterpret_cast<const uint16_t *>(p + L.o_col);
+      for (; e + 1 < e1; e += 2) {
+        s0 = fma(val[e], xw[col[e] & wmask], s0);
+        s1 = fma(val[e + 1], xw[col[e + 1] & wmask], s1);
+      }
+      if (e < e1) s0 = fma(val[e], xw[col[e] & wmask], s0);
+    } else {
+      const uint32_t *col = reinterpret_cast<const uint32_t *>(p + L.o_col);
+      for (; e + 1 < e1; e += 2) {
+        s0 = fma(val[e], xw[col[e] & wmask], s0);
+        s1 = fma(val[e + 1], xw[col[e + 1] & wmask], s1);
+      }
+      if (e < e1) s0 = fma(val[e], xw[col[e] & wmask], s0);
+    }
+    tsh[lane] = lane < (int)nr ? q0 - (s0 + s1) : VT(0);
+    __syncwarp();
+    const VT x = apply_row(m, tsh);
+    if (lane < (int)nr) {
+      xw[(row0 + lane) & wmask] = x;
+      out[nd.begin + row0 + lane] = (OutT)x;
+    }
+    q0 = q1;
+    q1 = q2;
+    q2 = rhs(k + 3);
+    __syncwarp();  // slot and tsh free again
+    oc.advance(k + NB, lane);  // the lowest record index used below
+    if (k + NB < nb) {
+      if (lane == 0) fence_proxy_async();
+      issue(k + NB);
+    }
+    if (a.pf && k + a.pf < nb) {
+      const int64_t o0 = oc.get(k + a.pf), o1 = oc.get(k + a.pf + 1);
+      if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
+    }
+  }
+  if (!ok) {  // give up: wait (bounded) for the copies still in flight, one per slot
+    if (lane == 0) {
+      atomicOr(&g_solve_status, 1u);
+      for (int j = k; j < nb && j < k + NB; ++j) (void)mbar_wait(bar + j % NB, (uint32_t)(j / NB) & 1u);
+    }
+    __syncwarp();
+  }
+}
+
+template <typename VT>
+struct PipeArgs {
+  const NodeDesc *nodes;
+  int node0;         // piece = node0 + blockIdx.x
+  int bufbytes;      // bytes of a ring slot (16-aligned)
+  int ring;          // ring slots (4..8): records k, k+1, k+2 in use, the rest in flight
+  int maxchunk;      // most chunks of one block (chunk-sum buffer)
+  int pf;            // records prefetched into L2 ahead of use
+  const unsigned char *blocks;
+  const int64_t *blk_off;
+  const VT *acc;     // rhs minus external sums, or null: the stage reads `in`
+};
+
+// One thread block per piece: warp 0 solves, warp 1 reduces and streams the
+// records, warps 2.. gather.  One __syncthreads per step; in step s the
+// solver retires block s, the reducer prepares u for block s+1, the
+// gatherers sum the far entries of block s+2.  The piece's right-hand side
+// and then its solution live in shared memory (xs).
+template <typename VT, typename InT, typename OutT, bool UPPER>
+__global__ void __launch_bounds__(512, 1) pipe_kernel(PipeArgs<VT> a, const InT *__restrict__ in,
+                                                      OutT *__restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int abort_flag;
+  const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int RING = a.ring, nb = nd.nblocks;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+  VT *tsh = reinterpret_cast<VT *>(smem + al16(8 * (size_t)RING));
+  VT *ubuf = tsh + BS;                    // [2][32]
+  VT *part = ubuf + 2 * BS;               // [2][maxchunk]
+  unsigned char *ring = reinterpret_cast<unsigned char *>(tsh) + al16(sizeof(VT) * (3 * BS + 2 * (size_t)a.maxchunk));
+  VT *xs = reinterpret_cast<VT *>(ring + (size_t)RING * a.bufbytes);
+  OffCache oc;
+  if (warp == 1) oc.init(a.blk_off + nd.blk0, nb, lane);
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int i = 0; i < RING; ++i) mbar_init(bar + i, 1);
+    fence_mbar_init();
+  }
+  for (int r = tid; r < nd.rows; r += blockDim.x) xs[r] = rhs_at(a.acc, in, nd.begin + r);
+  __syncthreads();
+  auto slot_of = [&](int k) { return ring + (size_t)(k % RING) * a.bufbytes; };
+  auto issue = [&](int k) {  // warp 1: record k into its slot
+    const int64_t o0 = oc.get(k), o1 = oc.get(k + 1);
+    if (lane == 0) bulk_load(slot_of(k), a.blocks + o0, (uint32_t)(o1 - o0), bar + k % RING);
+  };
+  if (warp == 1)
+    for (int k = 0; k < RING - 3 && k < nb; ++k) issue(k);
+  auto wait_rec = [&](int k) {
+    if (!mbar_wait(bar + k % RING, (uint32_t)(k / RING) & 1u)) {
+      atomicOr(&g_solve_status, 1u);
+      abort_flag = 1;
+      return false;
+    }
+    return true;
+  };
+  VT m[BS];  // solver: inverse row of its next block
+  uint32_t issued = (uint32_t)min(RING - 3, nb);
+  for (int s = -2; s < nb; ++s) {
+    const bool stop = abort_flag != 0;  // read after the last barrier: uniform
+    if (!stop) {
+      if (warp == 0) {
+        if (s >= 0) {
+          const unsigned char *p = slot_of(s);
+          const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
+          const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
+          const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
+          const uint32_t nr = h0.x, row0 = h0.y, prow0 = h0.z, n1 = h1.x;
+          const unsigned char *n1c = p + h2.y;
+          const VT *n1v = reinterpret_cast<const VT *>(p + h2.z);
+          VT t0 = lane < (int)nr ? ubuf[(s & 1) * BS + lane] : VT(0), t1 = 0;
+          uint32_t j = 0;
+          for (; j + 1 < n1; j += 2) {
+            t0 = fma(-n1v[j * BS + lane], xs[prow0 + n1c[j * BS + lane]], t0);
+            t1 = fma(-n1v[(j + 1) * BS + lane], xs[prow0 + n1c[(j + 1) * BS + lane]], t1);
+          }
+          if (j < n1) t0 = fma(-n1v[j * BS + lane], xs[prow0 + n1c[j * BS + lane]], t0);
+          tsh[lane] = lane < (int)nr ? t0 + t1 : VT(0);
+          __syncwarp();
+          const VT x = apply_row(m, tsh);
+          if (lane < (int)nr) {
+            xs[row0 + lane] = x;
+            out[nd.begin + row0 + lane] = (OutT)x;
+          }
+        }
+        if (s + 1 >= 0 && s + 1 < nb) {  // next block's inverse row, ahead of the barrier
+          if (wait_rec(s + 1)) load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(slot_of(s + 1) + 64), lane, m);
+        }
+      } else if (warp == 1) {
+        // stream: record s-1+RING into the slot of record s-1 (retired last step)
+        const int k = s - 1 + RING;
+        oc.advance(a.pf ? min(k, s + a.pf) : k, lane);  // the lowest record index used this step
+        if (k >= RING - 3 && k < nb) {
+          if (lane == 0) fence_proxy_async();
+          issue(k);
+          issued = (uint32_t)(k + 1);
+        }
+        if (a.pf && s + a.pf >= 0 && s + a.pf < nb) {
+          const int64_t o0 = oc.get(s + a.pf), o1 = oc.get(s + a.pf + 1);
+          if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
+        }
+        const int bk = s + 1;  // reducer: u of block s+1
+        if (bk >= 0 && bk < nb && wait_rec(bk)) {
+          const unsigned char *p = slot_of(bk);
+          const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
+          const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
+          const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
+          const uint4 h3 = *reinterpret_cast<const uint4 *>(p + 48);
+          const uint32_t nr = h0.x, row0 = h0.y, pprow0 = h0.w, n2 = h1.y;
+          const unsigned char *n2c = p + h2.w;
+          const VT *n2v = reinterpret_cast<const VT *>(p + h3.x);
+          const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h3.y);
+          const VT *pb = part + (size_t)(bk & 1) * a.maxchunk;
+          VT u0 = lane < (int)nr ? xs[row0 + lane] : VT(0), u1 = 0;
+          uint32_t c = crow[lane];
+          const uint32_t c1 = crow[lane + 1];
+          for (; c + 1 < c1; c += 2) {
+            u0 -= pb[c];
+            u1 -= pb[c + 1];
+          }
+          if (c < c1) u0 -= pb[c];
+          uint32_t j = 0;
+          for (; j + 1 < n2; j += 2) {
+            u0 = fma(-n2v[j * BS + lane], xs[pprow0 + n2c[j * BS + lane]], u0);
+            u1 = fma(-n2v[(j + 1) * BS + lane], xs[pprow0 + n2c[(j + 1) * BS + lane]], u1);
+          }
+          if (j < n2) u0 = fma(-n2v[j * BS + lane], xs[pprow0 + n2c[j * BS + lane]], u0);
+          ubuf[(bk & 1) * BS + lane] = lane < (int)nr ? u0 + u1 : VT(0);
+        }
+      } else {
+        const int bk = s + 2;  // gatherers: far sums of block s+2
+        if (bk < nb && wait_rec(bk)) {
+          const unsigned char *p = slot_of(bk);
+          const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
+          const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
+          const uint4 h3 = *reinterpret_cast<const uint4 *>(p + 48);
+          const uint32_t nchunk = h1.z, clen = h1.w, csz = h2.x;
+          const int g = tid - 64;
+          if (g < (int)nchunk) {
+            const VT *fv = reinterpret_cast<const VT *>(p + h3.w);
+            VT s0 = 0, s1 = 0;
+            uint32_t jj = 0, at = (uint32_t)g;
+            if (csz == 2) {
+              const uint16_t *fc = reinterpret_cast<const uint16_t *>(p + h3.z);
+              for (; jj + 1 < clen; jj += 2, at += 2 * nchunk) {
+                s0 = fma(fv[at], xs[fc[at]], s0);
+                s1 = fma(fv[at + nchunk], xs[fc[at + nchunk]], s1);
+              }
+              if (jj < clen) s0 = fma(fv[at], xs[fc[at]], s0);
+            } else {
+              const uint32_t *fc = reinterpret_cast<const uint32_t *>(p + h3.z);
+              for (; jj + 1 < clen; jj += 2, at += 2 * nchunk) {
+                s0 = fma(fv[at], xs[fc[at]], s0);
+                s1 = fma(fv[at + nchunk], xs[fc[at + nchunk]], s1);
+              }
+              if (jj < clen) s0 = fma(fv[at], xs[fc[at]], s0);
+            }
+            part[(size_t)(bk & 1) * a.maxchunk + g] = s0 + s1;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (abort_flag && warp == 1 && lane == 0) {
+    // copies that may still be in flight: the last RING issued, one per slot
+    for (int j = max(0, (int)issued - RING); j < (int)issued; ++j)
+      (void)mbar_wait(bar + j % RING, (uint32_t)(j / RING) & 1u);
+  }
+}
+
 }  // namespace
 
 // ---- plan construction ---------------------------------------------------------------
@@ -931,16 +1326,12 @@ __global__ void __launch_bounds__(256, 1) team_k_kernel(TeamArgs<VT> a, OutT *ou
 // SM count of the current device (a scheduling heuristic only: without a
 // device, as in host-side plan checks, the GB300's 152 is assumed).
 static int sm_count() {
-  static int count = 0;
-  if (!count) {
-    int dev = 0, c = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess &&
-        cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && c > 0)
-      count = c;
-    else
-      count = 152;
-  }
-  return count;
+  int dev = 0, c = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+      c > 0)
+    return c;
+  (void)cudaGetLastError();
+  return 152;
 }
 
 // Host copy of one direction's stream (tests/stream_emulator.cu executes it on the CPU).
@@ -952,108 +1343,142 @@ struct HostStreamCopy {
   std::vector<int32_t> ext_ci;
   std::vector<double> ext_v;
   std::vector<int> stage_ptr;
-  std::vector<int> stage_team;
+  std::vector<int> stage_fmt;
+  std::vector<int> stage_window;
 };
+
+constexpr size_t kSmemCap = 220 * 1024;      // dynamic shared memory a launch may use
+constexpr int kW2Ring = 4;                   // warp format: record slots per warp
+constexpr int kW2WindowMax = 8192;           // warp format: most rows in a window
+constexpr size_t kW2WarpBudget = 56 * 1024;  // warp format: shared memory of one warp (at least 4 warps per SM)
+constexpr int kPipeRingCut = 6;              // pipeline format: ring the pieces are cut for (launch: up to 8)
+
+// Pipeline team size of a stage with `pieces` pieces: 16 warps where at
+// most one piece runs per SM, fewer (several teams per SM) beyond.
+static int pipe_warps_for(int pieces, int sms) { return pieces <= sms ? 16 : pieces <= 2 * sms ? 8 : 4; }
 
 static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
                               const std::vector<double> &v, int64_t n, const std::vector<TreeNode> &tnodes,
-                              bool upper, bool fp32, int team_mode, int kwidth, StreamDir &D, cudaStream_t s,
+                              bool upper, bool fp32, int fmt_mode, int kwidth, StreamDir &D, cudaStream_t s,
                               HostStreamCopy *host_copy = nullptr) {
   const size_t vsz = fp32 ? 4 : 8;
-  const size_t row_bytes = vsz * (size_t)kwidth;  // a piece's unknowns per row in shared memory
-  if (kwidth > 1) team_mode = 2;                  // several right-hand sides: team format only
-  // Pieces: a node is cut into consecutive pieces (whole blocks) so that the
-  // shared memory of its solver holds the piece's unknowns plus its record
-  // buffers: two for the warp format (more at launch where room is left),
-  // the ring and the chunk sums for the team format.  The bound of a block
-  // record counts every entry of its rows that lies in the node but outside
-  // the block (an upper bound of its sparse part).
-  const size_t budget = 200 * 1024;
+  const int sms = sm_count();
   int maxdepth = 1;
   for (auto &nd : tnodes) maxdepth = std::max(maxdepth, nd.depth);
-  // One team size for all depths: doubling the team where few pieces run
-  // measured slower (the extra helpers' barrier and shared-memory traffic
-  // cost more than their shorter chunks save).
-  auto team_warps_of = [&](int) { return D.team_warps; };
-  // team format for separators (few, long chains), warp format for leaves
-  auto team_depth = [&](int depth) {
-    if (team_mode == 0) return false;
-    return team_mode == 2 || depth < maxdepth;
-  };
   struct Piece {
     int64_t b, e;
-    bool team;
-    int warps;
+    int fmt;     // FMT_WARP, FMT_PIPE or FMT_KTEAM
+    int warps;   // pipeline / k-team: warps of the team
+    int window;  // warp format: window rows
   };
-  auto cut_node = [&](int64_t b, int64_t e, bool team, int warps) {
-    const int helper_threads = 32 * (warps - 1);
-    std::vector<Piece> out;
+  // entries of rows [r0, r1) with columns in [b, e) outside the rows' block: an
+  // upper bound of a block record's sparse part
+  auto block_counts = [&](int64_t b, int64_t e) {
     const int64_t nb = (e - b + BS - 1) / BS;
-    std::vector<size_t> recb(nb);
+    std::vector<size_t> cnt(nb);
     parallel_for(nb, [&](int64_t k0, int64_t k1) {
       for (int64_t k = k0; k < k1; ++k) {
         const int64_t r0 = b + k * BS, r1 = std::min(e, r0 + BS);
-        size_t cnt = 0;
+        size_t c = 0;
         for (int64_t i = r0; i < r1; ++i)
-          for (int64_t q = rp[i]; q < rp[i + 1]; ++q) cnt += (ci[q] >= b && ci[q] < e && (ci[q] < r0 || ci[q] >= r1));
-        recb[k] = team ? team_record_bound(cnt, helper_threads, vsz, e - b > 65535 ? 4 : 2)
-                       : 16 + al16(4 * (BS + 1)) + al16(4 * cnt) + al16(vsz * cnt) + al16(vsz * TRI);
+          for (int64_t q = rp[i]; q < rp[i + 1]; ++q) c += (ci[q] >= b && ci[q] < e && (ci[q] < r0 || ci[q] >= r1));
+        cnt[k] = c;
       }
     }, 256);
-    const size_t fixed = !team ? 0
-                         : kwidth > 1 ? 2 * (size_t)BS * KW * vsz
-                                      : 2 * al16((size_t)(helper_threads + BS) * vsz);
-    const size_t nrec = team ? TEAM_RING : 2;
+    return cnt;
+  };
+  // cut [b, e) into pieces of whole blocks whose shared memory fits:
+  // fixed + nrec * record + rows * row_bytes <= cap (pieces of one node are
+  // solved one after another; entries into earlier pieces become external)
+  auto cut = [&](int64_t b, int64_t e, const std::vector<size_t> &recb, size_t fixed, size_t nrec, size_t row_bytes,
+                 int64_t max_rows, size_t cap, std::vector<std::pair<int64_t, int64_t>> &out) {
+    const int64_t nb = (e - b + BS - 1) / BS;
     int64_t k = 0;
     while (k < nb) {
       int64_t k1 = k;
       size_t mx = 0;
       while (k1 < nb) {
-        const size_t m2 = std::max(mx, recb[k1]);
+        const size_t m2 = std::max(mx, al16(recb[k1]));
         const int64_t rows = std::min(e, b + (k1 + 1) * BS) - (b + k * BS);
-        if (k1 > k && (fixed + nrec * al16(m2) + (size_t)rows * row_bytes > budget || rows > 65535)) break;
+        if (k1 > k && (fixed + nrec * m2 + (size_t)rows * row_bytes > cap || rows > max_rows)) break;
         mx = m2;
         ++k1;
       }
-      // a single block may run with the smallest ring (3 records: no copy in
-      // flight across a step) rather than fall back to the warp format
-      const size_t nmin = team ? 3 : 2;
-      if (fixed + nmin * al16(mx) + (size_t)(std::min(e, b + k1 * BS) - (b + k * BS)) * row_bytes > budget)
-        throw Error(RCHOL_ERR_INTERNAL, "a 32-row block of G is too dense for the shared-memory solve");
-      out.push_back(Piece{b + k * BS, std::min(e, b + k1 * BS), team, warps});
+      const int64_t rows = std::min(e, b + k1 * BS) - (b + k * BS);
+      if (fixed + nrec * mx + (size_t)rows * row_bytes > cap) return false;
+      out.push_back({b + k * BS, std::min(e, b + k1 * BS)});
       k = k1;
     }
-    return out;
+    return true;
+  };
+  // longest row-column distance inside [b, e)
+  auto reach_of = [&](int64_t b, int64_t e) {
+    int64_t r = 0;
+    for (int64_t i = b; i < e; ++i)
+      for (int64_t q = rp[i]; q < rp[i + 1]; ++q)
+        if (ci[q] >= b && ci[q] < e) r = std::max<int64_t>(r, std::abs(i - (int64_t)ci[q]));
+    return r;
+  };
+  auto pow2_at_least = [](int64_t x) {
+    int64_t w = 64;
+    while (w < x) w <<= 1;
+    return w;
   };
   std::vector<Piece> pieces;
-  std::vector<char> team_failed(maxdepth + 1, 0);
   D.stage_ptr.assign(1, 0);
   for (int st = 0; st < maxdepth; ++st) {
     const int depth = upper ? st + 1 : maxdepth - st;
-    std::vector<std::vector<Piece>> by_index;  // piece j of every node of this depth
-    bool retry_depth = false;
-    for (auto &nd : tnodes) {
-      if (nd.depth != depth) continue;
-      const int64_t b = nd.begin, e = std::min(nd.end, n);
-      if (e <= b) continue;
-      std::vector<Piece> ps;
-      bool team = team_depth(depth) && !team_failed[depth];
-      try {
-        ps = cut_node(b, e, team, team_warps_of(depth));
-      } catch (const Error &) {
-        if (!team || kwidth > 1) throw;
-        // a block too dense for the team ring: this depth uses the warp format
-        team_failed[depth] = true;
-        retry_depth = true;
-        break;
+    std::vector<std::pair<int64_t, int64_t>> nodes;
+    for (auto &nd : tnodes)
+      if (nd.depth == depth && std::min(nd.end, n) > nd.begin) nodes.push_back({nd.begin, std::min(nd.end, n)});
+    if (nodes.empty()) continue;
+    const int P = (int)nodes.size();
+    int fmt = kwidth > 1 ? FMT_KTEAM : fmt_mode == 0 ? FMT_WARP : fmt_mode == 2 ? FMT_PIPE : P >= 2 * sms ? FMT_WARP : FMT_PIPE;
+    std::vector<std::vector<Piece>> per_node(P);
+    for (int attempt = 0; attempt < 2; ++attempt) {
+      bool ok = true;
+      for (int j = 0; j < P && ok; ++j) {
+        const int64_t b = nodes[j].first, e = nodes[j].second;
+        const std::vector<size_t> cnt = block_counts(b, e);
+        std::vector<std::pair<int64_t, int64_t>> rng;
+        per_node[j].clear();
+        if (fmt == FMT_WARP) {
+          std::vector<size_t> recb(cnt.size());
+          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = w2_record_bound(cnt[k], vsz, e - b > 65535 ? 4 : 2);
+          const int64_t W = std::min<int64_t>(pow2_at_least(std::min<int64_t>(reach_of(b, e) + BS + 1, e - b)),
+                                              kW2WindowMax);
+          const size_t fixed = al16(8 * kW2Ring) + BS * vsz;
+          // rows per piece bounded by the window: a piece of at most W rows
+          // never reads outside it, whatever the node's reach
+          ok = cut(b, e, recb, fixed + (size_t)W * vsz, kW2Ring, 0, W >= kW2WindowMax ? W : INT64_MAX,
+                   kW2WarpBudget, rng);
+          for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_WARP, 1, (int)W});
+        } else if (fmt == FMT_PIPE) {
+          const int warps = pipe_warps_for(P, sms);
+          const int gth = 32 * (warps - 2);
+          std::vector<size_t> recb(cnt.size());
+          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = pipe_record_bound(cnt[k], gth, vsz, e - b > 65535 ? 4 : 2);
+          const size_t fixed = al16(8 * 8) + al16(vsz * (3 * BS + 2 * (size_t)gth));
+          ok = cut(b, e, recb, fixed, kPipeRingCut, vsz, 1 << 30, kSmemCap, rng);
+          for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_PIPE, warps, 0});
+        } else {
+          const int warps = 8, hth = 32 * (warps - 1);
+          std::vector<size_t> recb(cnt.size());
+          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = team_record_bound(cnt[k], hth, vsz, e - b > 65535 ? 4 : 2);
+          const size_t fixed = 2 * (size_t)BS * KW * vsz;
+          ok = cut(b, e, recb, fixed, TEAM_RING, vsz * KW, 65535, kSmemCap, rng);
+          for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_KTEAM, warps, 0});
+        }
       }
+      if (ok) break;
+      if (fmt != FMT_WARP) throw Error(RCHOL_ERR_INTERNAL, "a 32-row block of G is too dense for the shared-memory solve");
+      fmt = FMT_PIPE;  // records too large for a warp's share: this depth in the pipeline format
+    }
+    std::vector<std::vector<Piece>> by_index;  // piece j of every node of this depth
+    for (auto &ps : per_node) {
       if (upper) std::reverse(ps.begin(), ps.end());  // backward: last piece first
       if (by_index.size() < ps.size()) by_index.resize(ps.size());
       for (size_t j = 0; j < ps.size(); ++j) by_index[j].push_back(ps[j]);
-    }
-    if (retry_depth) {
-      --st;  // the same depth again, in the warp format
-      continue;
     }
     for (auto &grp : by_index) {
       for (auto &pc : grp) pieces.push_back(pc);
@@ -1095,11 +1520,17 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   std::vector<int32_t> chunks(np, 0);
   parallel_for(np, [&](int64_t k0, int64_t k1) {
     for (int64_t k = k0; k < k1; ++k) {
-      if (pieces[k].team)
-        build_team_piece(rp, ci, v, pieces[k].b, pieces[k].e, upper, vsz, 32 * (pieces[k].warps - 1), kwidth > 1,
-                         built[k], chunks[k]);
-      else
-        build_piece(rp, ci, v, pieces[k].b, pieces[k].e, upper, vsz, built[k]);
+      const Piece &pc = pieces[k];
+      if (pc.fmt == FMT_WARP) {
+        int64_t reach = 0;
+        build_w2_piece(rp, ci, v, pc.b, pc.e, upper, vsz, built[k], reach);
+        if (reach + BS >= pc.window && pc.window < pc.e - pc.b)
+          throw Error(RCHOL_ERR_INTERNAL, "warp-format window shorter than the piece's reach");
+      } else if (pc.fmt == FMT_PIPE) {
+        build_pipe_piece(rp, ci, v, pc.b, pc.e, upper, vsz, 32 * (pc.warps - 2), built[k], chunks[k]);
+      } else {
+        build_team_piece(rp, ci, v, pc.b, pc.e, upper, vsz, 32 * (pc.warps - 1), true, built[k], chunks[k]);
+      }
     }
   }, 1);
   std::vector<NodeDesc> desc(np);
@@ -1128,32 +1559,37 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   // stages
   D.stage_rows.clear();
   D.stage_maxrec.clear();
-  D.stage_team.clear();
+  D.stage_fmt.clear();
   D.stage_warps.clear();
   D.stage_chunks.clear();
+  D.stage_window.clear();
+  D.stage_ext.clear();
   D.stage_ext_lanes.clear();
   D.stage_row_ptr.assign(1, 0);
   D.steps = 0;
   std::vector<int32_t> srows;
   for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
-    int rows = 0, maxrec = 16, steps = 0, maxchunk = 0;
+    int rows = 0, maxrec = 16, steps = 0, maxchunk = 0, window = 0;
     int64_t ext = 0, nrow = 0;
     for (int k = D.stage_ptr[st]; k < D.stage_ptr[st + 1]; ++k) {
       rows = std::max(rows, desc[k].rows);
       maxrec = std::max(maxrec, desc[k].maxrec);
       steps = std::max(steps, desc[k].nblocks);
       maxchunk = std::max(maxchunk, desc[k].maxchunk);
+      window = std::max(window, pieces[k].window);
       for (int64_t i = desc[k].begin; i < desc[k].begin + desc[k].rows; ++i) srows.push_back((int32_t)i);
       ext += ext_rp[desc[k].begin + desc[k].rows] - ext_rp[desc[k].begin];
       nrow += desc[k].rows;
     }
-    const bool team = D.stage_ptr[st + 1] > D.stage_ptr[st] && pieces[D.stage_ptr[st]].team;
+    const Piece &p0 = pieces[D.stage_ptr[st]];
     const double avg = nrow ? (double)ext / (double)nrow : 0.0;
     D.stage_rows.push_back(rows);
     D.stage_maxrec.push_back(maxrec);
-    D.stage_team.push_back(team ? 1 : 0);
-    D.stage_warps.push_back(D.stage_ptr[st + 1] > D.stage_ptr[st] ? pieces[D.stage_ptr[st]].warps : D.team_warps);
+    D.stage_fmt.push_back(p0.fmt);
+    D.stage_warps.push_back(p0.warps);
     D.stage_chunks.push_back(std::max(1, maxchunk));
+    D.stage_window.push_back(window);
+    D.stage_ext.push_back(ext > 0 ? 1 : 0);
     D.stage_ext_lanes.push_back(avg < 6 ? 1 : avg < 24 ? 4 : avg < 96 ? 8 : 32);
     D.stage_row_ptr.push_back((int64_t)srows.size());
     D.steps += steps;
@@ -1168,7 +1604,8 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     host_copy->ext_ci = eci;
     host_copy->ext_v = ev;
     host_copy->stage_ptr = D.stage_ptr;
-    host_copy->stage_team = D.stage_team;
+    host_copy->stage_fmt = D.stage_fmt;
+    host_copy->stage_window = D.stage_window;
     return;
   }
   D.blocks.upload(all.data(), all.size(), s);
@@ -1202,21 +1639,18 @@ static void build_streams_width(const rchol_factor_s &F, int kwidth, StreamDir &
   F.lci.download(ci.data(), nnz, s);
   F.lv.download(v.data(), nnz, s);
   RCHOL_CUDA(cudaStreamSynchronize(s));
-  // Schedule knobs (tuning only; every setting solves exactly the same
-  // system): RCHOL_TRSV_TEAM = 0 warp format everywhere, 1 team format for
-  // separators, 2 team format everywhere (default); RCHOL_TRSV_TEAM_WARPS =
-  // warps of a team (2..8, default 8).
-  int team_mode = 2, team_warps = 8;
-  if (const char *e = getenv("RCHOL_TRSV_TEAM")) team_mode = std::max(0, std::min(2, atoi(e)));
-  if (const char *e = getenv("RCHOL_TRSV_TEAM_WARPS")) team_warps = std::max(2, std::min(8, atoi(e)));
-  if (kwidth > 1) team_warps = 8;
-  fwd.team_warps = bwd.team_warps = team_warps;
-  build_dir_streams(rp, ci, v, n, F.nodes, false, fp32, team_mode, kwidth, fwd, s);
+  // Schedule knob (tuning only; every setting solves exactly the same
+  // system): RCHOL_TRSV_FORMAT = 0 warp format everywhere, 1 by stage
+  // (default: warp format where a depth has many nodes, pipeline format
+  // at the top of the tree), 2 pipeline format everywhere.
+  int fmt_mode = 1;
+  if (const char *e = getenv("RCHOL_TRSV_FORMAT")) fmt_mode = std::max(0, std::min(2, atoi(e)));
+  build_dir_streams(rp, ci, v, n, F.nodes, false, fp32, fmt_mode, kwidth, fwd, s);
   F.urp.download(rp.data(), n + 1, s);
   F.uci.download(ci.data(), nnz, s);
   F.uv.download(v.data(), nnz, s);
   RCHOL_CUDA(cudaStreamSynchronize(s));
-  build_dir_streams(rp, ci, v, n, F.nodes, true, fp32, team_mode, kwidth, bwd, s);
+  build_dir_streams(rp, ci, v, n, F.nodes, true, fp32, fmt_mode, kwidth, bwd, s);
 }
 
 void build_streams(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
@@ -1248,92 +1682,111 @@ static void once_per_device(std::once_flag (&flags)[kMaxDevices], Fn &&set) {
   std::call_once(flags[dev], std::forward<Fn>(set));
 }
 
+// External sums of one stage: acc_i = in_i - sum of row i's entries outside
+// its piece, for the stage's rows (1, 4, 8 or 32 lanes per row).
+template <typename VT, typename InT, typename OutT>
+static void launch_ext(const StreamDir &D, size_t st, const VT *ext_v, const InT *in, const OutT *out, VT *acc,
+                       cudaStream_t s) {
+  const int64_t r0 = D.stage_row_ptr[st], r1 = D.stage_row_ptr[st + 1], nr = r1 - r0;
+  const int lanes = D.stage_ext_lanes[st];
+  const unsigned eg = (unsigned)((nr * lanes + 255) / 256);
+  switch (lanes) {
+    case 1:
+      ext_kernel<VT, InT, OutT><<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
+      break;
+    case 4:
+      ext_lanes_kernel<VT, InT, OutT, 4><<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
+      break;
+    case 8:
+      ext_lanes_kernel<VT, InT, OutT, 8><<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
+      break;
+    default:
+      ext_lanes_kernel<VT, InT, OutT, 32><<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
+      break;
+  }
+  note_launch();
+}
+
+// Records prefetched into L2 ahead of use (0: none): RCHOL_TRSV_PREFETCH.
+static int prefetch_distance(int fallback) {
+  static const int v = [] {
+    const char *e = getenv("RCHOL_TRSV_PREFETCH");
+    return e ? std::max(0, std::min(28, atoi(e))) : -1;
+  }();
+  return v < 0 ? fallback : v;
+}
+
 template <typename VT, typename InT, typename OutT>
 static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *out, VT *acc, cudaStream_t s) {
   const StreamDir &D = upper ? P.sbwd : P.sfwd;
   constexpr bool f64 = sizeof(VT) == 8;
   const VT *ext_v = reinterpret_cast<const VT *>(f64 ? (const void *)D.ext_v64.p : (const void *)D.ext_v32.p);
-  const int smem_cap = 220 * 1024;
   static std::once_flag attr_once[kMaxDevices];
   once_per_device(attr_once, [&] {
-    RCHOL_CUDA(cudaFuncSetAttribute(block_kernel<VT, OutT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    smem_cap));
-    RCHOL_CUDA(cudaFuncSetAttribute(block_kernel<VT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    smem_cap));
-    RCHOL_CUDA(cudaFuncSetAttribute(team_kernel<VT, OutT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    smem_cap));
-    RCHOL_CUDA(cudaFuncSetAttribute(team_kernel<VT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    smem_cap));
+    RCHOL_CUDA(cudaFuncSetAttribute(w2_kernel<VT, InT, OutT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmemCap));
+    RCHOL_CUDA(cudaFuncSetAttribute(w2_kernel<VT, InT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmemCap));
+    RCHOL_CUDA(cudaFuncSetAttribute(pipe_kernel<VT, InT, OutT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmemCap));
+    RCHOL_CUDA(cudaFuncSetAttribute(pipe_kernel<VT, InT, OutT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kSmemCap));
   });
-  BlockArgs<VT> a;
-  a.nodes = D.nodes.p;
-  a.blocks = D.blocks.p;
-  a.blk_off = D.blk_off.p;
-  a.acc = acc;
-  a.upper = upper;
-  TeamArgs<VT> ta;
-  ta.nodes = D.nodes.p;
-  ta.blocks = D.blocks.p;
-  ta.blk_off = D.blk_off.p;
-  ta.acc = acc;
+  const int sms = sm_count();
   for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
     const int pieces = D.stage_ptr[st + 1] - D.stage_ptr[st];
     if (!pieces) continue;
-    const int64_t r0 = D.stage_row_ptr[st], r1 = D.stage_row_ptr[st + 1], nr = r1 - r0;
-    const int lanes = D.stage_ext_lanes[st];
-    const unsigned eg = (unsigned)((nr * lanes + 255) / 256);
-    switch (lanes) {
-      case 1:
-        ext_kernel<VT, InT, OutT><<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
-        break;
-      case 4:
-        ext_lanes_kernel<VT, InT, OutT, 4>
-            <<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
-        break;
-      case 8:
-        ext_lanes_kernel<VT, InT, OutT, 8>
-            <<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
-        break;
-      default:
-        ext_lanes_kernel<VT, InT, OutT, 32>
-            <<<eg, 256, 0, s>>>(D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc);
-        break;
+    // stages without external entries read the right-hand side directly
+    const VT *src_acc = nullptr;
+    if (D.stage_ext[st]) {
+      launch_ext<VT, InT, OutT>(D, st, ext_v, in, out, acc, s);
+      src_acc = acc;
     }
-    note_launch();
-    const size_t xs_bytes = (size_t)D.stage_rows[st] * sizeof(VT);
-    if (D.stage_team[st]) {
-      ta.node0 = D.stage_ptr[st];
-      ta.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
-      ta.maxchunk = D.stage_chunks[st];
-      const size_t fixed = al16((size_t)ta.maxchunk * sizeof(VT)) + 2 * BS * sizeof(VT) + xs_bytes;
-      // the deepest ring that fits (records arrive ring-3 steps ahead of use)
-      // where few pieces share the GPU; where many do, they hide each
-      // other's latency and shared memory goes to residency instead
-      int ring = pieces > 2 * sm_count() ? 5 : TEAM_RING_MAX;
-      while (ring > 3 && fixed + (size_t)ring * ta.bufbytes > (size_t)smem_cap) --ring;
-      ta.ring = ring;
-      const size_t bytes = (size_t)ring * ta.bufbytes + fixed;
-      if (bytes > (size_t)smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
-      const unsigned threads = 32u * (unsigned)D.stage_warps[st];
-      if (upper) team_kernel<VT, OutT, true><<<pieces, threads, bytes, s>>>(ta, out);
-      else team_kernel<VT, OutT, false><<<pieces, threads, bytes, s>>>(ta, out);
-    } else {
+    const size_t bufbytes = al16((size_t)D.stage_maxrec[st]);
+    if (D.stage_fmt[st] == FMT_WARP) {
+      W2Args<VT> a;
+      a.nodes = D.nodes.p;
       a.node0 = D.stage_ptr[st];
       a.node1 = D.stage_ptr[st + 1];
-      a.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
-      // deep rings for the few long chains at the top of the tree (latency),
-      // shallower ones where many pieces share an SM (they hide each other)
-      int nbuf = pieces >= 256 ? 4 : 6;
-      while (nbuf > 2 && (size_t)nbuf * a.bufbytes + xs_bytes > (size_t)smem_cap) --nbuf;
-      a.nbuf = nbuf;
-      a.per_warp = (int)al16((size_t)nbuf * a.bufbytes + xs_bytes);
-      int wpb = std::max(1, std::min(4, smem_cap / a.per_warp));
-      if (a.per_warp > smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
-      wpb = std::min(wpb, pieces);
+      a.blocks = D.blocks.p;
+      a.blk_off = D.blk_off.p;
+      a.acc = src_acc;
+      a.nbuf = kW2Ring;
+      a.bufbytes = (int)bufbytes;
+      a.wmask = (uint32_t)D.stage_window[st] - 1u;
+      a.per_warp = (int)al16(al16(8 * (size_t)kW2Ring) + BS * sizeof(VT) + (size_t)kW2Ring * bufbytes +
+                             (size_t)D.stage_window[st] * sizeof(VT));
+      a.pf = prefetch_distance(0);
+      if (a.pf) a.pf = std::max(a.pf, kW2Ring);  // the offset cache holds records k+NB .. k+NB+63
+      if ((size_t)a.per_warp > kSmemCap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
+      int wpb = std::max(1, std::min(8, (int)(kSmemCap / (size_t)a.per_warp)));
+      // spread small stages over the SMs rather than packing few blocks
+      while (wpb > 1 && (pieces + wpb - 1) / wpb < sms) wpb >>= 1;
       a.wpb = wpb;
-      const int grid = (pieces + wpb - 1) / wpb;
-      if (upper) block_kernel<VT, OutT, true><<<grid, 32 * wpb, (size_t)a.per_warp * wpb, s>>>(a, out);
-      else block_kernel<VT, OutT, false><<<grid, 32 * wpb, (size_t)a.per_warp * wpb, s>>>(a, out);
+      const unsigned grid = (unsigned)((pieces + wpb - 1) / wpb);
+      const size_t bytes = (size_t)a.per_warp * wpb;
+      if (upper) w2_kernel<VT, InT, OutT, true><<<grid, 32 * wpb, bytes, s>>>(a, in, out);
+      else w2_kernel<VT, InT, OutT, false><<<grid, 32 * wpb, bytes, s>>>(a, in, out);
+    } else {
+      PipeArgs<VT> a;
+      a.nodes = D.nodes.p;
+      a.node0 = D.stage_ptr[st];
+      a.blocks = D.blocks.p;
+      a.blk_off = D.blk_off.p;
+      a.acc = src_acc;
+      a.bufbytes = (int)bufbytes;
+      a.maxchunk = D.stage_chunks[st];
+      a.pf = prefetch_distance(pieces <= sms ? 24 : 0);
+      const int warps = D.stage_warps[st];
+      const size_t fixed0 = al16(sizeof(VT) * (3 * BS + 2 * (size_t)a.maxchunk)) + (size_t)D.stage_rows[st] * sizeof(VT);
+      int ring = 8;
+      while (ring > 4 && al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes > kSmemCap) --ring;
+      a.ring = ring;
+      const size_t bytes = al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes;
+      if (bytes > kSmemCap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
+      const unsigned threads = 32u * (unsigned)warps;
+      if (upper) pipe_kernel<VT, InT, OutT, true><<<pieces, threads, bytes, s>>>(a, in, out);
+      else pipe_kernel<VT, InT, OutT, false><<<pieces, threads, bytes, s>>>(a, in, out);
     }
     note_launch();
     RCHOL_CUDA(cudaGetLastError());

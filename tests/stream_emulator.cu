@@ -3,18 +3,21 @@
 // Builds the forward (G) and backward (G^T) streams of a factor with the
 // library's own host-side builder (build_dir_streams, host copy, no device),
 // then executes them on the CPU in the order the kernels do: per stage the
-// external entries, then per piece block after block -- in the team format
-// the helpers' far sums of block k+1 from the unknowns solved before block k,
-// the solver's near entries from block k-1, and the packed inverse.  Every
-// column a record reads must already be solved at that point (a record that
-// reads ahead would race on the GPU); the results are compared with plain
-// substitution on the CSR of G.
+// external entries, then per piece block after block.  Warp format: every
+// column a row reads must be solved and still held by the window of solved
+// values.  Pipeline format: the kernel's three-step schedule -- in step s the
+// gatherers sum block s+2's far entries from columns solved before step s,
+// the reducer prepares block s+1 with its entries in block s-1, the solver
+// retires block s with its entries in block s-1.  32-wide (k-team) format:
+// helpers one block ahead, the solver with the previous block.  A record that
+// reads a column not solved at that point would race on the GPU and fails
+// the check; the results are compared with plain substitution on the CSR of G.
 //
-//   stream_emulator <dir> <team_mode 0|1|2> <precision 0=FP64|1=FP32> <kwidth 1|32>
+//   stream_emulator <dir> <format 0=warp|1=by stage|2=pipeline> <precision 0=FP64|1=FP32> <kwidth 1|32>
 //
 // <dir> holds hdr.bin (n, nnz, len(result_idx)), rp.bin / ci.bin / v.bin (CSR
 // of G^T: int64, int32, f64) and ridx.bin (result_idx, int64).  Prints one
-// line "ok rel_fwd rel_bwd team_pieces steps" or "FAIL ..." (exit code 1).
+// line "ok rel_fwd rel_bwd team_pieces steps warp_pieces" or "FAIL ..." (exit code 1).
 
 #include "../rchol_gb300/csrc/trsv.cu"
 
@@ -84,9 +87,25 @@ void apply_inverse(const unsigned char *minv, const VT *t, VT *x, bool upper) {
   }
 }
 
+// x = T^-1 t with the row-quad packed inverse of a warp- or pipeline-format record
+template <typename VT>
+void apply_tinv(const unsigned char *tinv, const VT *t, VT *x, bool upper) {
+  for (int r = 0; r < BS; ++r) {
+    VT s = 0;
+    for (int q = tq_lo(r, upper); q <= tq_hi(r, upper); ++q)
+      for (int j = 0; j < 4; ++j) {
+        const int c = 4 * q + j;
+        const VT m = ld<VT>(tinv, 4 * (size_t)(tq_off(r, upper) + q - tq_lo(r, upper)) + j);
+        if ((upper ? c < r : c > r) && m != (VT)0) fail("inverse entry outside the triangle", r, c);
+        s += m * t[c];
+      }
+    x[r] = s;
+  }
+}
+
 template <typename VT>
 std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &rhs, int64_t n, bool upper,
-                            bool slot_major, long &team_pieces) {
+                            long &team_pieces, long &warp_pieces) {
   std::vector<double> out(n, 0.0);
   std::vector<char> done(n, 0);
   const uint32_t vsz = sizeof(VT);
@@ -106,7 +125,7 @@ std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &
         acc[i] = (VT)rhs[i] - s;
       }
     }
-    const bool team = H.stage_team[st] != 0;
+    const int fmt = H.stage_fmt[st];
     for (int k = H.stage_ptr[st]; k < H.stage_ptr[st + 1]; ++k) {
       const NodeDesc &nd = H.desc[k];
       std::vector<VT> xs(nd.rows);
@@ -114,33 +133,141 @@ std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &
       for (int r = 0; r < nd.rows; ++r) xs[r] = acc[nd.begin + r];
       auto rec = [&](int b) {
         const int64_t o = H.blk_off[nd.blk0 + b];
-        if (o < 0 || o >= (int64_t)H.blocks.size()) fail("record offset", (long)o, b);
+        if (o < 0 || o >= (int64_t)H.blocks.size() || (o & 15)) fail("record offset", (long)o, b);
         return H.blocks.data() + o;
       };
-      if (!team) {
+      auto rec_len = [&](int b) { return H.blk_off[nd.blk0 + b + 1] - H.blk_off[nd.blk0 + b]; };
+      auto finish = [&](int b, uint32_t nr, uint32_t row0, const VT *x) {
+        if (row0 + nr > (uint32_t)nd.rows) fail("block rows outside the piece", row0, b);
+        for (uint32_t r = 0; r < nr; ++r) {
+          if (solved_at[row0 + r] >= 0) fail("row solved twice", row0 + r, b);
+          xs[row0 + r] = x[r];
+          solved_at[row0 + r] = b;
+        }
+      };
+      if (fmt == FMT_WARP) {
+        // the window of solved values: slot i % W holds the row written last
+        const int64_t W = H.stage_window[st];
+        if (W < 64 || (W & (W - 1))) fail("window size", (long)W, k);
+        std::vector<int64_t> slot(W, -1);
+        ++warp_pieces;
         for (int b = 0; b < nd.nblocks; ++b) {
           const unsigned char *p = rec(b);
           uint32_t hdr[4];
           std::memcpy(hdr, p, 16);
-          const uint32_t nr = hdr[0], nent = hdr[1], row0 = hdr[2], csz = hdr[3];
-          const size_t o_col = 16 + al16(4 * (BS + 1)), o_val = o_col + al16((size_t)csz * nent),
-                       o_min = o_val + al16((size_t)vsz * nent);
-          uint32_t off[BS + 1];
-          std::memcpy(off, p + 16, sizeof(off));
+          const uint32_t nr = hdr[0], row0 = hdr[1], nent = hdr[2], csz = hdr[3];
+          const W2Layout L = w2_layout(nent, csz, vsz);
+          if ((int64_t)L.len != rec_len(b)) fail("warp record length", (long)L.len, b);
+          if ((int)L.len > nd.maxrec) fail("record above the piece's maximum", (long)L.len, nd.maxrec);
+          uint16_t off[BS + 1];
+          std::memcpy(off, p + L.o_eoff, sizeof(off));
+          if (off[BS] != nent) fail("warp entry offsets", off[BS], nent);
           VT t[BS] = {}, x[BS];
           for (uint32_t r = 0; r < nr; ++r) {
-            VT s = 0;
+            VT s0 = 0, s1 = 0;
             for (uint32_t e = off[r]; e < off[r + 1]; ++e) {
-              const uint32_t c = col_at(p + o_col, e, csz);
+              const uint32_t c = col_at(p + L.o_col, e, csz);
               if (c >= (uint32_t)nd.rows || solved_at[c] < 0) fail("warp-format column not yet solved", c, b);
-              s += ld<VT>(p + o_val, e) * xs[c];
+              if (slot[c & (W - 1)] != (int64_t)c) fail("warp-format column no longer in the window", c, b);
+              ((e - off[r]) & 1 ? s1 : s0) += ld<VT>(p + L.o_val, e) * xs[c];
             }
-            t[r] = xs[row0 + r] - s;
+            t[r] = xs[row0 + r] - (s0 + s1);
           }
-          apply_inverse<VT>(p + o_min, t, x, upper);
-          for (uint32_t r = 0; r < nr; ++r) {
-            xs[row0 + r] = x[r];
-            solved_at[row0 + r] = b;
+          apply_tinv<VT>(p + L.o_tinv, t, x, upper);
+          finish(b, nr, row0, x);
+          for (uint32_t r = 0; r < nr; ++r) slot[(row0 + r) & (W - 1)] = row0 + r;
+        }
+      } else if (fmt == FMT_PIPE) {
+        ++team_pieces;
+        // the kernel's schedule: in step s the gatherers sum block s+2's far
+        // entries, the reducer prepares u of block s+1, the solver retires block s
+        std::vector<std::vector<VT>> part(2);
+        std::vector<VT> u(2 * BS, (VT)NAN);
+        const int nb = nd.nblocks;
+        auto hdr_of = [&](int b, uint32_t h[16]) {
+          const unsigned char *p = rec(b);
+          std::memcpy(h, p, 64);
+          const PipeLayout L = pipe_layout(h[4], h[5], h[6], h[7], h[8], vsz);
+          if ((int64_t)L.len != rec_len(b)) fail("pipeline record length", (long)L.len, b);
+          if ((int)L.len > nd.maxrec) fail("record above the piece's maximum", (long)L.len, nd.maxrec);
+          if (h[9] != L.o_n1c || h[10] != L.o_n1v || h[11] != L.o_n2c || h[12] != L.o_n2v || h[13] != L.o_crow ||
+              h[14] != L.o_fc || h[15] != L.o_fv)
+            fail("pipeline record offsets", b, 0);
+          if ((int)h[6] > nd.maxchunk) fail("chunks above the piece's maximum", h[6], nd.maxchunk);
+          return p;
+        };
+        for (int s = -2; s < nb; ++s) {
+          std::vector<VT> newpart;
+          if (s + 2 < nb) {  // gatherers
+            uint32_t h[16];
+            const unsigned char *p = hdr_of(s + 2, h);
+            const uint32_t nchunk = h[6], clen = h[7], csz = h[8];
+            newpart.assign(nchunk, 0);
+            for (uint32_t c = 0; c < nchunk; ++c) {
+              VT s0 = 0, s1 = 0;
+              for (uint32_t j = 0; j < clen; ++j) {
+                const size_t at = (size_t)j * nchunk + c;
+                const uint32_t col = col_at(p + h[14], at, csz);
+                const VT val = ld<VT>(p + h[15], at);
+                if (col >= (uint32_t)nd.rows) fail("far column outside the piece", col, s + 2);
+                if (val != (VT)0 && (solved_at[col] < 0 || solved_at[col] > s - 1))
+                  fail("far column not solved before the step", col, s + 2);
+                (j & 1 ? s1 : s0) += val * xs[col];
+              }
+              newpart[c] = s0 + s1;
+            }
+          }
+          std::vector<VT> newu;
+          if (s + 1 >= 0 && s + 1 < nb) {  // reducer
+            const int bk = s + 1;
+            uint32_t h[16];
+            const unsigned char *p = hdr_of(bk, h);
+            const uint32_t nr = h[0], row0 = h[1], pprow0 = h[3], n2 = h[5];
+            uint16_t crow[BS + 1];
+            std::memcpy(crow, p + h[13], sizeof(crow));
+            if (crow[BS] != h[6]) fail("chunk rows", crow[BS], h[6]);
+            const std::vector<VT> &pb = part[bk & 1];
+            if (pb.size() != h[6]) fail("chunk sums not prepared", bk, (long)pb.size());
+            newu.assign(BS, 0);
+            for (uint32_t r = 0; r < nr; ++r) {
+              VT u0 = xs[row0 + r], u1 = 0;
+              if (solved_at[row0 + r] >= 0) fail("reducer row already solved", row0 + r, bk);
+              for (uint32_t c = crow[r]; c < crow[r + 1]; ++c) ((c - crow[r]) & 1 ? u1 : u0) -= pb[c];
+              for (uint32_t j = 0; j < n2; ++j) {
+                const uint32_t c = p[h[11] + (size_t)j * BS + r];
+                const VT val = ld<VT>(p + h[12], (size_t)j * BS + r);
+                if (c >= (uint32_t)BS) fail("distance-2 column", c, bk);
+                if (val != (VT)0 && (bk < 2 || pprow0 + c >= (uint32_t)nd.rows || solved_at[pprow0 + c] != bk - 2))
+                  fail("distance-2 column not in block k-2", c, bk);
+                (j & 1 ? u1 : u0) -= val * xs[pprow0 + c];
+              }
+              newu[r] = u0 + u1;
+            }
+          }
+          if (s >= 0) {  // solver
+            uint32_t h[16];
+            const unsigned char *p = hdr_of(s, h);
+            const uint32_t nr = h[0], row0 = h[1], prow0 = h[2], n1 = h[4];
+            VT t[BS] = {}, x[BS];
+            for (uint32_t r = 0; r < nr; ++r) {
+              VT t0 = u[(s & 1) * BS + r], t1 = 0;
+              if (std::isnan((double)t0)) fail("u not prepared", r, s);
+              for (uint32_t j = 0; j < n1; ++j) {
+                const uint32_t c = p[h[9] + (size_t)j * BS + r];
+                const VT val = ld<VT>(p + h[10], (size_t)j * BS + r);
+                if (c >= (uint32_t)BS) fail("distance-1 column", c, s);
+                if (val != (VT)0 && (s < 1 || prow0 + c >= (uint32_t)nd.rows || solved_at[prow0 + c] != s - 1))
+                  fail("distance-1 column not in block k-1", c, s);
+                (j & 1 ? t1 : t0) -= val * xs[prow0 + c];
+              }
+              t[r] = t0 + t1;
+            }
+            apply_tinv<VT>(p + 64, t, x, upper);
+            finish(s, nr, row0, x);
+          }
+          if (s + 2 < nb) part[(s + 2) & 1] = newpart;
+          if (s + 1 >= 0 && s + 1 < nb) {
+            for (int r = 0; r < BS; ++r) u[((s + 1) & 1) * BS + r] = newu[r];
           }
         }
       } else {
@@ -153,9 +280,8 @@ std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &
             uint32_t h[16];
             std::memcpy(h, p, 64);
             const uint32_t nr1 = h[0], row01 = h[1], nchunk = h[4], clen = h[5], csz = h[6];
-            const TeamLayout L = team_layout(h[3], slot_major ? h[7] : 0, nchunk, clen, csz, vsz);
-            if ((int64_t)L.len != H.blk_off[nd.blk0 + b + 2] - H.blk_off[nd.blk0 + b + 1])
-              fail("team record length", (long)L.len, b + 1);
+            const TeamLayout L = team_layout(h[3], h[7], nchunk, clen, csz, vsz);
+            if ((int64_t)L.len != rec_len(b + 1)) fail("team record length", (long)L.len, b + 1);
             if (h[11] != L.o_fcol || h[12] != L.o_fval || h[13] != L.o_min) fail("team record offsets", b + 1, 0);
             if ((int)nchunk > nd.maxchunk) fail("chunks above the piece's maximum", nchunk, nd.maxchunk);
             std::vector<VT> part(nchunk);
@@ -181,26 +307,19 @@ std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &
               u[((b + 1) & 1) * BS + r] = r < nr1 ? xs[row01 + r] - (f0 + f1) : (VT)0;
             }
           }
-          // solver: block b, near entries from block b-1 (still in registers)
+          // solver: block b, near entries from block b-1 (slot-major)
           const unsigned char *p = rec(b);
           uint32_t h[16];
           std::memcpy(h, p, 64);
           const uint32_t nr = h[0], row0 = h[1], prow0 = h[2], nmax = h[7];
-          const TeamLayout L = team_layout(h[3], slot_major ? nmax : 0, h[4], h[5], h[6], vsz);
-          uint16_t noff[BS + 1];
-          if (!slot_major) {
-            std::memcpy(noff, p + L.o_noff, sizeof(noff));
-            if (noff[BS] != h[3]) fail("near offsets", noff[BS], h[3]);
-          }
+          const TeamLayout L = team_layout(h[3], nmax, h[4], h[5], h[6], vsz);
           VT t[BS] = {}, x[BS];
           for (uint32_t r = 0; r < nr; ++r) {
             const VT ur = b == 0 ? xs[row0 + r] : u[(b & 1) * BS + r];
             if (std::isnan((double)ur)) fail("u not prepared", r, b);
-            const uint32_t cnt = slot_major ? nmax : (uint32_t)(noff[r + 1] - noff[r]);
-            if (cnt > nmax) fail("near entries above nmax", r, b);
             VT s0 = 0, s1 = 0;
-            for (uint32_t j = 0; j < cnt; ++j) {
-              const size_t at = slot_major ? (size_t)j * BS + r : (size_t)noff[r] + j;
+            for (uint32_t j = 0; j < nmax; ++j) {
+              const size_t at = (size_t)j * BS + r;
               const uint32_t c = p[L.o_ncol + at];
               const VT val = ld<VT>(p + L.o_nval, at);
               if (c >= (uint32_t)BS) fail("near column", c, b);
@@ -211,10 +330,7 @@ std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &
           }
           apply_inverse<VT>(p + L.o_min, t, x, upper);
           for (int r = 0; r < BS; ++r) xprev[r] = r < (int)nr ? x[r] : (VT)0;
-          for (uint32_t r = 0; r < nr; ++r) {
-            xs[row0 + r] = x[r];
-            solved_at[row0 + r] = b;
-          }
+          finish(b, nr, row0, x);
         }
       }
       for (int r = 0; r < nd.rows; ++r) {
@@ -233,7 +349,7 @@ std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &
 
 int main(int argc, char **argv) {
   if (argc < 5) {
-    std::printf("FAIL usage: stream_emulator <dir> <team_mode> <precision> <kwidth>\n");
+    std::printf("FAIL usage: stream_emulator <dir> <format> <precision> <kwidth>\n");
     return 1;
   }
   const std::string dir = argv[1];
@@ -292,13 +408,11 @@ int main(int argc, char **argv) {
   }
   StreamDir Df, Db;
   HostStreamCopy Hf, Hb;
-  Df.team_warps = Db.team_warps = 8;
   build_dir_streams(lrp, lci, lv, n, nodes, false, fp32, team_mode, kwidth, Df, 0, &Hf);
   build_dir_streams(rp, ci, v, n, nodes, true, fp32, team_mode, kwidth, Db, 0, &Hb);
-  long tf = 0, tb = 0;
-  const bool slot_major = kwidth > 1;
-  const auto ye = fp32 ? emulate<float>(Hf, b, n, false, slot_major, tf) : emulate<double>(Hf, b, n, false, slot_major, tf);
-  const auto ze = fp32 ? emulate<float>(Hb, y, n, true, slot_major, tb) : emulate<double>(Hb, y, n, true, slot_major, tb);
+  long tf = 0, tb = 0, wf = 0, wb = 0;
+  const auto ye = fp32 ? emulate<float>(Hf, b, n, false, tf, wf) : emulate<double>(Hf, b, n, false, tf, wf);
+  const auto ze = fp32 ? emulate<float>(Hb, y, n, true, tb, wb) : emulate<double>(Hb, y, n, true, tb, wb);
   double ey = 0, ny = 0, ez = 0, nz = 0;
   for (int64_t i = 0; i < n; ++i) {
     ey += (ye[i] - y[i]) * (ye[i] - y[i]);
@@ -306,6 +420,7 @@ int main(int argc, char **argv) {
     ez += (ze[i] - z[i]) * (ze[i] - z[i]);
     nz += z[i] * z[i];
   }
-  std::printf("ok %.3e %.3e %ld %ld\n", std::sqrt(ey / ny), std::sqrt(ez / nz), tf + tb, (long)(Df.steps + Db.steps));
+  std::printf("ok %.3e %.3e %ld %ld %ld\n", std::sqrt(ey / ny), std::sqrt(ez / nz), tf + tb, (long)(Df.steps + Db.steps),
+              wf + wb);
   return 0;
 }

@@ -5,7 +5,8 @@ code of rchol_gb300/csrc/trsv.cu) into a CPU program, builds the forward and
 backward streams of oracle factors (device-contract mode, i.e. the GPU's G)
 and executes them in the kernels' order: every record may only read unknowns
 solved at that point, and the result must equal plain substitution.  Warp,
-mixed and team formats, FP64 and FP32 values, single and 32-wide records."""
+pipeline and staged (warp format for depths with many nodes, pipeline at
+the top) formats, FP64 and FP32 values, single and 32-wide records."""
 
 import os
 import shutil
@@ -60,21 +61,22 @@ def factor_dir(request, O):
     return out
 
 
-@pytest.mark.parametrize("team_mode,precision,kwidth", [(0, 0, 1), (1, 0, 1), (2, 0, 1), (2, 1, 1), (2, 0, 32),
-                                                         (2, 1, 32)],
-                         ids=["warp-fp64", "mixed-fp64", "team-fp64", "team-fp32", "wide-fp64", "wide-fp32"])
-def test_streams_solve_exactly(emulator, factor_dir, team_mode, precision, kwidth):
-    res = subprocess.run([emulator, factor_dir, str(team_mode), str(precision), str(kwidth)], capture_output=True,
+@pytest.mark.parametrize("fmt,precision,kwidth", [(0, 0, 1), (0, 1, 1), (1, 0, 1), (1, 1, 1), (2, 0, 1), (2, 1, 1),
+                                                   (2, 0, 32), (2, 1, 32)],
+                         ids=["warp-fp64", "warp-fp32", "staged-fp64", "staged-fp32", "pipe-fp64", "pipe-fp32",
+                              "wide-fp64", "wide-fp32"])
+def test_streams_solve_exactly(emulator, factor_dir, fmt, precision, kwidth):
+    res = subprocess.run([emulator, factor_dir, str(fmt), str(precision), str(kwidth)], capture_output=True,
                          text=True, timeout=300)
     line = res.stdout.strip().splitlines()[-1] if res.stdout.strip() else res.stderr
     assert res.returncode == 0 and line.startswith("ok"), line
-    _, rel_fwd, rel_bwd, team_pieces, steps = line.split()
+    _, rel_fwd, rel_bwd, team_pieces, steps, warp_pieces = line.split()
     tol = 1e-12 if precision == 0 else 1e-4  # FP32 values and arithmetic
     assert float(rel_fwd) < tol and float(rel_bwd) < tol, line
-    if team_mode == 2:
-        assert int(team_pieces) > 0
-    if team_mode == 0:
-        assert int(team_pieces) == 0
+    if fmt == 2:
+        assert int(team_pieces) > 0 and int(warp_pieces) == 0
+    if fmt == 0 and kwidth == 1:  # depths whose blocks are too dense for a warp's share fall back to the pipeline
+        assert int(warp_pieces) > 0
 
 
 def test_emulator_catches_a_misordered_tree(emulator, O):
