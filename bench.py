@@ -45,7 +45,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=256, help="grid side")
-    p.add_argument("--leaves", type=int, default=2048, help="nested-dissection subdomains")
+    p.add_argument("--leaves", type=int, default=0,
+                   help="nested-dissection subdomains (0: the tuned count cached for this shape, else 2048)")
     p.add_argument("--tol", type=float, default=1e-8)
     p.add_argument("--maxit", type=int, default=200)
     p.add_argument("--seed", type=int, default=0)
@@ -180,6 +181,12 @@ def run_gb300(args, rank, local, world, pg):
     L = _lib.lib()
     A, b, t_gen = build_problem(args)
     n = A.shape[0]
+    from rchol_gb300 import tuning
+
+    leaves_source = "argument"
+    if args.leaves <= 0:
+        args.leaves = tuning.subdomains_for(n, A.nnz, R.PREC_FP32)
+        leaves_source = "tuning cache" if tuning.load_cache().get(tuning._key(n, A.nnz, R.PREC_FP32)) else "default"
     t0 = time.time()
     tree = R.Tree.build(A.indptr, A.indices, args.leaves)
     perm, part = tree.arrays()
@@ -194,6 +201,7 @@ def run_gb300(args, rank, local, world, pg):
     t_factor = time.time() - t0
     setup_split = F64.setup_times()  # factor_gpu = eliminate + assemble + plan (+ the extended Laplacian)
     F32 = R.Factor.compute(Ad, tree, seed=args.seed, precision=R.PREC_FP32)
+    knobs32, knobs64 = F32.tune(), F64.tune()  # launch choices timed on each factor
     nnzG = F64.nnz
     nnzA = A.nnz
     bp = np.ascontiguousarray(b[perm])
@@ -316,7 +324,8 @@ def run_gb300(args, rank, local, world, pg):
         "config": {
             "workload": f"PCG to {args.tol:g}, 7-point log-normal Laplacian {args.n}^3 (n={n}, nnz(A)={nnzA}), "
                         f"rchol G (nnz={nnzG}) stored and applied in FP32",
-            "grid": args.n, "leaves": args.leaves, "tol": args.tol,
+            "grid": args.n, "leaves": args.leaves, "leaves_from": leaves_source, "tol": args.tol,
+            "tuned_launch": {"fp32": knobs32, "fp64": knobs64},
             "l2": "inputs larger than L2 (A %.2f GB, G %.2f GB)" % (nnzA * 12 / 1e9, nnzG * 8 / 1e9),
             "parallelism": f"replicas x{world}",
         },
@@ -504,13 +513,58 @@ def run_differentiation(args, dev):
     rel_l = float(np.linalg.norm(A @ lam - (xh - xt0)) / np.linalg.norm(xh - xt0))
     g_host = -(lam[ei] - lam[ej]) * (xh[ei] - xh[ej])
     g_err = float(np.abs(gw - g_host).max() / np.abs(g_host).max())
+    ref = differentiation_reference(A, b0, xt0, w0, ei, ej, gw, lam, rng)
     return {"workload": "2D 5-point 1024^2 (n=1,048,576, 2,095,104 edges), log-uniform weights [1e-2, 1e2], "
                         "shift 1e-4, loss 0.5||x - x_target||^2, FP64 G, PCG to 1e-10",
             "ms_forward": round(ms_f, 2), "iters_forward": it_f,
             "ms_backward": round(ms_b, 2), "iters_adjoint": it_b,
             "relres_host_fp64_x": rel_x, "relres_host_fp64_adjoint": rel_l,
-            "edge_grad_vs_host_formula": g_err,
+            "edge_grad_vs_host_formula": g_err, "independent_check": ref,
             "setup_s": round(setup, 1), "first_step_with_factor_s": round(factor_s, 1)}
+
+
+def differentiation_reference(A, b, xt, w, ei, ej, gw, lam_gpu, rng, samples=200, rel_step=1e-6):
+    """An independent reference for the 1024^2 gradient: one sparse LU of
+    A(w) (scipy SuperLU) gives x and lambda = A^-1 (x - x_target) by direct
+    solves.  (1) dL/db = lambda and dL/dw_e = -(lambda_i - lambda_j)(x_i - x_j)
+    from the LU solves, on all of b and on `samples` random edges, against
+    the GPU's adjoint-PCG gradients.  (2) FP64 central finite differences of
+    the loss on the same edges, step h = rel_step * w_e: a change of one edge
+    weight is the rank-one update A + h d d^T (d = u_i - u_j), so each
+    perturbed solve is exact through Sherman-Morrison with z = A^-1 d (one LU
+    solve per edge), and L(w + h) - L(w - h) is formed from the two updates
+    without cancellation against L itself."""
+    import scipy.sparse.linalg as spla
+
+    t0 = time.time()
+    lu = spla.splu(A.tocsc(), permc_spec="MMD_AT_PLUS_A")
+    x = lu.solve(b)
+    r = x - xt
+    lam = lu.solve(r)
+    pick = rng.choice(len(ei), samples, replace=False)
+    gi, gj = ei[pick], ej[pick]
+    g_lu = -(lam[gi] - lam[gj]) * (x[gi] - x[gj])
+    fd = np.zeros(samples)
+    n = A.shape[0]
+    for k in range(samples):
+        d = np.zeros(n)
+        d[gi[k]], d[gj[k]] = 1.0, -1.0
+        z = lu.solve(d)
+        dx, dz = x[gi[k]] - x[gj[k]], z[gi[k]] - z[gj[k]]
+        h = rel_step * w[pick[k]]
+        zr, zz = float(z @ r), float(z @ z)
+        dL = []
+        for sgn in (1.0, -1.0):
+            c = sgn * h * dx / (1.0 + sgn * h * dz)  # x(w +- h) = x - c z
+            dL.append(-c * zr + 0.5 * c * c * zz)      # L(w +- h) - L(w)
+        fd[k] = (dL[0] - dL[1]) / (2 * h)
+    scale = np.abs(g_lu).max()
+    return {"edges": samples, "fd_rel_step": rel_step, "lu_s": round(time.time() - t0, 1),
+            "relres_lu_x": float(np.linalg.norm(A @ x - b) / np.linalg.norm(b)),
+            "grad_b_vs_lu": float(np.linalg.norm(lam_gpu - lam) / np.linalg.norm(lam)),
+            "grad_w_vs_lu": float(np.abs(gw[pick] - g_lu).max() / scale),
+            "grad_w_vs_fd": float(np.abs(gw[pick] - fd).max() / scale),
+            "lu_vs_fd": float(np.abs(g_lu - fd).max() / scale)}
 
 
 def cpu_baseline(args, Ap, bp, F64, it64):
@@ -593,6 +647,15 @@ def run_reference(args, rank, world):
     O = oracle.Oracle()
     threads = os.cpu_count() or 1
     A, b, _ = build_problem(args)
+    if args.leaves <= 0:  # the gb300 arm's count: tuned for this shape, else 2048 (no GPU library needed)
+        import json
+
+        try:
+            with open(os.path.join(ROOT, "rchol_gb300", "tuning_cache.json")) as f:
+                ent = json.load(f).get(f"n={A.shape[0]},nnz={A.nnz},prec=fp32")
+        except (OSError, ValueError):
+            ent = None
+        args.leaves = int(ent["subdomains"]) if ent else 2048
     A3 = (A.indptr.astype(np.uint64), A.indices.astype(np.uint64), A.data)
     t0 = time.time()
     perm, ridx = O.order(A3, args.leaves)
@@ -621,7 +684,8 @@ def run_reference(args, rank, world):
         "data": "synthetic (same seeds as the gb300 arm)",
         "config": {"workload": f"PCG to {args.tol:g}, 7-point log-normal Laplacian {args.n}^3, reference rchol G "
                                f"(nnz={len(G[1])}, {args.leaves} subdomains, the gb300 arm's count)",
-                   "grid": args.n, "leaves": args.leaves, "tol": args.tol, "same_config": True},
+                   "grid": args.n, "leaves": args.leaves, "leaves_from": leaves_source, "tol": args.tol,
+            "tuned_launch": {"fp32": knobs32, "fp64": knobs64}, "same_config": True},
         "iters": int(iters), "relres": relres, "relres_host_fp64": ver, "nnz_G": int(len(G[1])),
         "first_solve_s": round(t_first, 1), "order_s": round(t_order, 1), "factor_s": round(t_factor, 1),
         "cpu_baseline": {"value": round(value, 1), "unit": "ms", "cores": threads, "kind": "port",

@@ -118,7 +118,10 @@ void rchol_gpu_matrix_destroy(rchol_matrix_t A);
 int rchol_gpu_factor(rchol_matrix_t A, rchol_tree_t tree, uint64_t seed, int precision,
                      rchol_factor_t *out);
 /* Load a factor computed elsewhere (e.g. by the reference): CSR of G^T with
- * the diagonal first in each row, as rchol() returns it. */
+ * the diagonal first in each row, as rchol() returns it.  Without `tree`, the
+ * nested-dissection structure is read off G's nonzero pattern (contiguous
+ * ranges whose rows only read inside them), so independent subtrees are still
+ * solved in parallel. */
 int rchol_gpu_factor_from_host(int64_t n, const int64_t *row_ptr, const int64_t *col_idx,
                                const double *val, rchol_tree_t tree, int precision,
                                rchol_factor_t *out);
@@ -128,6 +131,20 @@ int rchol_gpu_factor_precision(rchol_factor_t G);
 int rchol_gpu_factor_export(rchol_factor_t G, int64_t *row_ptr, int64_t *col_idx, double *val);
 /* Pivots d of the factorization (length n), G = L sqrt(D). */
 int rchol_gpu_factor_pivots(rchol_factor_t G, double *d);
+/* Shape of the triangular-solve plan of the forward (transpose = 0) or
+ * backward solve: stages (kernel pairs in sequence), pieces, and the
+ * sequential 32-row block steps on the critical path.  No counterpart in
+ * the reference. */
+int rchol_gpu_factor_plan_info(rchol_factor_t G, int transpose, int64_t *stages, int64_t *pieces, int64_t *steps);
+/* Autotuning of the solves on this factor: times the preconditioner with
+ * alternative launch choices (L2 prefetch distance and ring depth of the
+ * pipeline format, warps per thread block and prefetch of the warp format)
+ * and keeps the fastest for all later solves with G.  ms_before / ms_after:
+ * preconditioner time with the choices on entry / chosen; knobs (4 ints, may
+ * be NULL): pipeline prefetch, pipeline ring, warp-format warps per block,
+ * warp-format prefetch.  Allocates scratch, synchronises the device.  No
+ * counterpart in the reference. */
+int rchol_gpu_factor_tune(rchol_factor_t G, double *ms_before, double *ms_after, int *knobs);
 /* Wall time (seconds) of the set-up phases that made G: the elimination
  * kernels (0 for rchol_gpu_factor_from_host), the assembly of G (transpose,
  * row sort, FP32 copies) and the triangular-solve plan.  No counterpart in

@@ -50,6 +50,8 @@ SIGNATURES = [
     ("rchol_gpu_factor_pivots", C.c_int, [_vp, _dp]),
     ("rchol_gpu_factor_levels", C.c_int, [_vp, _i64p, _i64p]),
     ("rchol_gpu_factor_setup_times", C.c_int, [_vp, _dp, _dp, _dp]),
+    ("rchol_gpu_factor_plan_info", C.c_int, [_vp, C.c_int, _i64p, _i64p, _i64p]),
+    ("rchol_gpu_factor_tune", C.c_int, [_vp, _dp, _dp, C.POINTER(C.c_int)]),
     ("rchol_gpu_factor_destroy", None, [_vp]),
     ("rchol_gpu_pcg", C.c_int, [_vp, _vp, _dp, _dp, _i64, C.c_double, C.c_int, _dp, _ip]),
     ("rchol_gpu_pcg_d", C.c_int, [_vp, _vp, _vp, _vp, _i64, C.c_double, C.c_int, _dp, _ip, _vp]),
@@ -250,6 +252,22 @@ class Factor(Handle):
         f, b = _i64(), _i64()
         check(lib().rchol_gpu_factor_levels(self.ptr, C.byref(f), C.byref(b)))
         return f.value, b.value
+
+    def plan_info(self, transpose=False):
+        """(stages, pieces, sequential block steps) of the forward or backward solve plan."""
+        a, b, c = _i64(), _i64(), _i64()
+        check(lib().rchol_gpu_factor_plan_info(self.ptr, int(transpose), C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def tune(self):
+        """Times the solves with alternative launch choices on this factor and
+        keeps the fastest; returns the preconditioner times before and after
+        and the chosen values."""
+        b, a = C.c_double(), C.c_double()
+        k = (C.c_int * 4)()
+        check(lib().rchol_gpu_factor_tune(self.ptr, C.byref(b), C.byref(a), k))
+        return {"ms_before": b.value, "ms_after": a.value, "pipe_prefetch": k[0], "pipe_ring": k[1],
+                "warp_blocks": k[2], "warp_prefetch": k[3]}
 
     def setup_times(self):
         """Seconds spent in elimination, assembly of G and the solve plan."""

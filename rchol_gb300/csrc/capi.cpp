@@ -6,10 +6,13 @@
 #include <atomic>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 
 #include "common.hpp"
 #include "host.hpp"
+#include "plan.hpp"
+#include "tree_infer.hpp"
 
 namespace rchol {
 
@@ -238,7 +241,9 @@ int rchol_gpu_factor_from_host(int64_t n, const int64_t *row_ptr, const int64_t 
   F->n = n;
   F->nnz = row_ptr[n];
   F->precision = precision;
-  F->nodes = tree ? tree->nodes : trivial_nodes(n);
+  // without a tree (a G made elsewhere, or copied): the tree its nonzero
+  // pattern shows, so that independent subtrees are solved in parallel
+  F->nodes = tree ? tree->nodes : infer_factor_tree(n, row_ptr, col_idx);
   std::vector<int32_t> ci32(F->nnz);
   for (int64_t i = 0; i < F->nnz; ++i) ci32[i] = (int32_t)col_idx[i];
   cudaStream_t s = 0;
@@ -252,6 +257,33 @@ int rchol_gpu_factor_from_host(int64_t n, const int64_t *row_ptr, const int64_t 
 }
 
 int64_t rchol_gpu_factor_nnz(rchol_factor_t G) { return G ? G->nnz : -1; }
+
+int rchol_gpu_factor_plan_info(rchol_factor_t G, int transpose, int64_t *stages, int64_t *pieces, int64_t *steps) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(G && G->plan, "null factor");
+  const StreamDir &D = transpose ? G->plan->sbwd : G->plan->sfwd;
+  if (stages) *stages = (int64_t)D.stage_ptr.size() - 1;
+  if (pieces) *pieces = D.stage_ptr.empty() ? 0 : D.stage_ptr.back();
+  if (steps) *steps = D.steps;
+  API_END
+}
+
+int rchol_gpu_factor_tune(rchol_factor_t G, double *ms_before, double *ms_after, int *knobs) {
+  API_BEGIN
+  RCHOL_CHECK_ARG(G && G->plan, "null factor");
+  std::lock_guard<std::mutex> guard(G->plan->lock);
+  const std::pair<double, double> t = tune_solves(*G, *G->plan, 0);
+  if (ms_before) *ms_before = t.first;
+  if (ms_after) *ms_after = t.second;
+  if (knobs) {
+    const SolveKnobs &k = G->plan->knobs;
+    knobs[0] = k.pipe_pf;
+    knobs[1] = k.pipe_ring;
+    knobs[2] = k.w2_wpb;
+    knobs[3] = k.w2_pf;
+  }
+  API_END
+}
 
 int rchol_gpu_factor_setup_times(rchol_factor_t G, double *eliminate_s, double *assemble_s, double *plan_s) {
   API_BEGIN

@@ -3,6 +3,7 @@
 
 #include <memory>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "common.hpp"
@@ -103,8 +104,20 @@ struct SegWork {
   }
 };
 
+// Launch-time choices of the single-right-hand-side solves (trsv.cu).  Any
+// setting solves the same system with the same arithmetic; the tuner
+// (rchol_gpu_factor_tune) times alternatives on the factor itself.
+struct SolveKnobs {
+  int pipe_pf = 24;   // pipeline format: records prefetched into L2 ahead of use (0: none)
+  int w2_pf = 0;      // warp format: the same
+  int pipe_ring = 8;  // pipeline format: most ring slots (4..8)
+  int w2_wpb = 8;     // warp format: most warps (pieces) per thread block (1..8)
+};
+
 struct SolvePlan {
   std::mutex lock;  // solves on one factor are serialised (they share workspaces)
+  SolveKnobs knobs;
+  double tuned_ms = 0.0;  // preconditioner time with the tuned knobs (0: not tuned)
   std::vector<std::unique_ptr<PcgWork>> pcg;
   std::vector<std::unique_ptr<SegWork>> seg;
   StreamDir sfwd, sbwd;
@@ -127,5 +140,8 @@ void stream_trsv_k(const rchol_factor_s &F, const SolvePlan &P, bool upper, cons
                    const float *in32, double *out64, float *out32, int k, cudaStream_t s);
 void stream_trsv(const rchol_factor_s &F, const SolvePlan &P, bool upper, const double *in64,
                  const float *in32, double *out64, float *out32, cudaStream_t s);
+// Times the preconditioner under alternative SolveKnobs and keeps the
+// fastest; returns {ms with the knobs on entry, ms with the chosen ones}.
+std::pair<double, double> tune_solves(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s);
 
 }  // namespace rchol

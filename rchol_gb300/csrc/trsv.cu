@@ -753,15 +753,16 @@ __host__ __device__ inline PipeLayout pipe_layout(uint32_t n1, uint32_t n2, uint
   return L;
 }
 
-// Upper bound of a pipeline record whose block has `cnt` entries in earlier
-// blocks of its piece, for `gthreads` gatherer threads.
-inline size_t pipe_record_bound(size_t cnt, size_t gthreads, size_t vsz, size_t csz) {
+// Upper bound of a pipeline record whose block's rows have at most n1 / n2
+// entries in the previous block / the one before and `far` entries in older
+// blocks of its piece, for `gthreads` gatherer threads (cutting the node into
+// pieces only moves entries out of a record).
+inline size_t pipe_record_bound(uint32_t n1, uint32_t n2, size_t far, size_t gthreads, size_t vsz, size_t csz) {
   const size_t slots = gthreads > (size_t)BS ? gthreads - BS : 1;
-  const size_t clen = std::max<size_t>(1, (cnt + slots - 1) / slots);
-  const size_t padded = cnt + BS * clen;
-  const size_t nslot = (size_t)BS * std::min<size_t>(cnt, BS);
-  return 64 + vsz * 4 * TQ + 2 * (al16(nslot) + al16(vsz * nslot)) + al16(2 * (BS + 1)) + al16(csz * padded) +
-         al16(vsz * padded);
+  const size_t clen = std::max<size_t>(1, (far + slots - 1) / slots);
+  const size_t padded = far + BS * clen;
+  return 64 + vsz * 4 * TQ + al16((size_t)BS * n1) + al16(vsz * BS * n1) + al16((size_t)BS * n2) +
+         al16(vsz * BS * n2) + al16(2 * (BS + 1)) + al16(csz * padded) + al16(vsz * padded);
 }
 
 void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, const std::vector<double> &v,
@@ -1371,17 +1372,35 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     int warps;   // pipeline / k-team: warps of the team
     int window;  // warp format: window rows
   };
-  // entries of rows [r0, r1) with columns in [b, e) outside the rows' block: an
-  // upper bound of a block record's sparse part
+  // Per block of [b, e): its rows' entries with columns in [b, e) outside the
+  // block (an upper bound of the record's sparse part, whatever the pieces),
+  // split for the pipeline format into the most entries of one row in the
+  // previous block (n1) and the one before (n2, processing order) and the rest.
+  struct BlockCount {
+    size_t cnt = 0, far = 0;
+    uint32_t n1 = 0, n2 = 0;
+  };
   auto block_counts = [&](int64_t b, int64_t e) {
     const int64_t nb = (e - b + BS - 1) / BS;
-    std::vector<size_t> cnt(nb);
+    std::vector<BlockCount> cnt(nb);
     parallel_for(nb, [&](int64_t k0, int64_t k1) {
       for (int64_t k = k0; k < k1; ++k) {
         const int64_t r0 = b + k * BS, r1 = std::min(e, r0 + BS);
-        size_t c = 0;
-        for (int64_t i = r0; i < r1; ++i)
-          for (int64_t q = rp[i]; q < rp[i + 1]; ++q) c += (ci[q] >= b && ci[q] < e && (ci[q] < r0 || ci[q] >= r1));
+        const int64_t b1 = upper ? k + 1 : k - 1, b2 = upper ? k + 2 : k - 2;
+        BlockCount c;
+        for (int64_t i = r0; i < r1; ++i) {
+          uint32_t m1 = 0, m2 = 0;
+          for (int64_t q = rp[i]; q < rp[i + 1]; ++q) {
+            if (ci[q] < b || ci[q] >= e || (ci[q] >= r0 && ci[q] < r1)) continue;
+            ++c.cnt;
+            const int64_t cb = (ci[q] - b) / BS;
+            if (cb == b1) ++m1;
+            else if (cb == b2) ++m2;
+            else ++c.far;
+          }
+          c.n1 = std::max(c.n1, m1);
+          c.n2 = std::max(c.n2, m2);
+        }
         cnt[k] = c;
       }
     }, 256);
@@ -1439,12 +1458,12 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
       bool ok = true;
       for (int j = 0; j < P && ok; ++j) {
         const int64_t b = nodes[j].first, e = nodes[j].second;
-        const std::vector<size_t> cnt = block_counts(b, e);
+        const std::vector<BlockCount> cnt = block_counts(b, e);
         std::vector<std::pair<int64_t, int64_t>> rng;
         per_node[j].clear();
         if (fmt == FMT_WARP) {
           std::vector<size_t> recb(cnt.size());
-          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = w2_record_bound(cnt[k], vsz, e - b > 65535 ? 4 : 2);
+          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = w2_record_bound(cnt[k].cnt, vsz, e - b > 65535 ? 4 : 2);
           const int64_t W = std::min<int64_t>(pow2_at_least(std::min<int64_t>(reach_of(b, e) + BS + 1, e - b)),
                                               kW2WindowMax);
           const size_t fixed = al16(8 * kW2Ring) + BS * vsz;
@@ -1457,14 +1476,21 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
           const int warps = pipe_warps_for(P, sms);
           const int gth = 32 * (warps - 2);
           std::vector<size_t> recb(cnt.size());
-          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = pipe_record_bound(cnt[k], gth, vsz, e - b > 65535 ? 4 : 2);
+          for (size_t k = 0; k < cnt.size(); ++k)
+            recb[k] = pipe_record_bound(cnt[k].n1, cnt[k].n2, cnt[k].far, gth, vsz, e - b > 65535 ? 4 : 2);
           const size_t fixed = al16(8 * 8) + al16(vsz * (3 * BS + 2 * (size_t)gth));
+          // the ring the pieces are cut for; the smallest one (4) where even a
+          // single block's records would not fit a deeper ring
           ok = cut(b, e, recb, fixed, kPipeRingCut, vsz, 1 << 30, kSmemCap, rng);
+          if (!ok) {
+            rng.clear();
+            ok = cut(b, e, recb, fixed, 4, vsz, 1 << 30, kSmemCap, rng);
+          }
           for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_PIPE, warps, 0});
         } else {
           const int warps = 8, hth = 32 * (warps - 1);
           std::vector<size_t> recb(cnt.size());
-          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = team_record_bound(cnt[k], hth, vsz, e - b > 65535 ? 4 : 2);
+          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = team_record_bound(cnt[k].cnt, hth, vsz, e - b > 65535 ? 4 : 2);
           const size_t fixed = 2 * (size_t)BS * KW * vsz;
           ok = cut(b, e, recb, fixed, TEAM_RING, vsz * KW, 65535, kSmemCap, rng);
           for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_KTEAM, warps, 0});
@@ -1707,13 +1733,14 @@ static void launch_ext(const StreamDir &D, size_t st, const VT *ext_v, const InT
   note_launch();
 }
 
-// Records prefetched into L2 ahead of use (0: none): RCHOL_TRSV_PREFETCH.
-static int prefetch_distance(int fallback) {
+// Records prefetched into L2 ahead of use (0: none); RCHOL_TRSV_PREFETCH
+// overrides the plan's choice (experiments only).
+static int prefetch_distance(int planned) {
   static const int v = [] {
     const char *e = getenv("RCHOL_TRSV_PREFETCH");
     return e ? std::max(0, std::min(28, atoi(e))) : -1;
   }();
-  return v < 0 ? fallback : v;
+  return std::max(0, std::min(28, v < 0 ? planned : v));
 }
 
 template <typename VT, typename InT, typename OutT>
@@ -1756,10 +1783,10 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       a.wmask = (uint32_t)D.stage_window[st] - 1u;
       a.per_warp = (int)al16(al16(8 * (size_t)kW2Ring) + BS * sizeof(VT) + (size_t)kW2Ring * bufbytes +
                              (size_t)D.stage_window[st] * sizeof(VT));
-      a.pf = prefetch_distance(0);
+      a.pf = prefetch_distance(P.knobs.w2_pf);
       if (a.pf) a.pf = std::max(a.pf, kW2Ring);  // the offset cache holds records k+NB .. k+NB+63
       if ((size_t)a.per_warp > kSmemCap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
-      int wpb = std::max(1, std::min(8, (int)(kSmemCap / (size_t)a.per_warp)));
+      int wpb = std::max(1, std::min(std::max(1, std::min(8, P.knobs.w2_wpb)), (int)(kSmemCap / (size_t)a.per_warp)));
       // spread small stages over the SMs rather than packing few blocks
       while (wpb > 1 && (pieces + wpb - 1) / wpb < sms) wpb >>= 1;
       a.wpb = wpb;
@@ -1776,10 +1803,10 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       a.acc = src_acc;
       a.bufbytes = (int)bufbytes;
       a.maxchunk = D.stage_chunks[st];
-      a.pf = prefetch_distance(pieces <= sms ? 24 : 0);
+      a.pf = prefetch_distance(pieces <= sms ? P.knobs.pipe_pf : 0);
       const int warps = D.stage_warps[st];
       const size_t fixed0 = al16(sizeof(VT) * (3 * BS + 2 * (size_t)a.maxchunk)) + (size_t)D.stage_rows[st] * sizeof(VT);
-      int ring = 8;
+      int ring = std::max(4, std::min(8, P.knobs.pipe_ring));
       while (ring > 4 && al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes > kSmemCap) --ring;
       a.ring = ring;
       const size_t bytes = al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes;
@@ -1791,6 +1818,75 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
     note_launch();
     RCHOL_CUDA(cudaGetLastError());
   }
+}
+
+// ---- autotuning of the launch-time choices -----------------------------------------------
+
+std::pair<double, double> tune_solves(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {
+  const int64_t n = F.n;
+  const bool fp32 = F.precision == RCHOL_PREC_FP32;
+  DevBuf<double> r(n), z(n), y64(fp32 ? 0 : n);
+  DevBuf<float> y32(fp32 ? n : 0);
+  if (fp32) {
+    if (P.acc32.n < (size_t)n) P.acc32.alloc(n);
+  } else if (P.acc64.n < (size_t)n) {
+    P.acc64.alloc(n);
+  }
+  RCHOL_CUDA(cudaMemsetAsync(r.p, 0, r.bytes(), s));
+  cudaEvent_t e0, e1;
+  RCHOL_CUDA(cudaEventCreate(&e0));
+  RCHOL_CUDA(cudaEventCreate(&e1));
+  auto apply = [&] {
+    if (fp32) {
+      launch_streams<float, double, float>(P, false, r.p, y32.p, P.acc32.p, s);
+      launch_streams<float, float, double>(P, true, y32.p, z.p, P.acc32.p, s);
+    } else {
+      launch_streams<double, double, double>(P, false, r.p, y64.p, P.acc64.p, s);
+      launch_streams<double, double, double>(P, true, y64.p, z.p, P.acc64.p, s);
+    }
+  };
+  auto time_ms = [&] {
+    apply();  // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {
+      RCHOL_CUDA(cudaEventRecord(e0, s));
+      apply();
+      RCHOL_CUDA(cudaEventRecord(e1, s));
+      RCHOL_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      RCHOL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best = std::min(best, ms);
+    }
+    return (double)best;
+  };
+  const double before = time_ms();
+  double best = before;
+  // coordinate descent over the knobs, each from the current best
+  auto try_knob = [&](int SolveKnobs::*field, std::initializer_list<int> values) {
+    const int keep = P.knobs.*field;
+    int pick = keep;
+    for (int v : values) {
+      if (v == keep) continue;
+      P.knobs.*field = v;
+      const double ms = time_ms();
+      if (ms < best * 0.995) {
+        best = ms;
+        pick = v;
+      }
+    }
+    P.knobs.*field = pick;
+  };
+  try_knob(&SolveKnobs::pipe_pf, {0, 8, 16, 24});
+  try_knob(&SolveKnobs::pipe_ring, {4, 6, 8});
+  try_knob(&SolveKnobs::w2_wpb, {1, 2, 4, 8});
+  try_knob(&SolveKnobs::w2_pf, {0, 8, 16});
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // captured PCG iterations launched with the old choices
+  P.pcg.clear();
+  P.seg.clear();
+  P.tuned_ms = best;
+  return {before, best};
 }
 
 void stream_trsv(const rchol_factor_s &F, const SolvePlan &P, bool upper, const double *in64,

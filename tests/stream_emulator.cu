@@ -13,13 +13,15 @@
 // reads a column not solved at that point would race on the GPU and fails
 // the check; the results are compared with plain substitution on the CSR of G.
 //
-//   stream_emulator <dir> <format 0=warp|1=by stage|2=pipeline> <precision 0=FP64|1=FP32> <kwidth 1|32>
+//   stream_emulator <dir> <format 0=warp|1=by stage|2=pipeline> <precision 0=FP64|1=FP32> <kwidth 1|32> [infer]
 //
 // <dir> holds hdr.bin (n, nnz, len(result_idx)), rp.bin / ci.bin / v.bin (CSR
-// of G^T: int64, int32, f64) and ridx.bin (result_idx, int64).  Prints one
+// of G^T: int64, int32, f64) and ridx.bin (result_idx, int64); with "infer"
+// the tree is read off G's pattern instead (tree_infer.hpp).  Prints one
 // line "ok rel_fwd rel_bwd team_pieces steps warp_pieces" or "FAIL ..." (exit code 1).
 
 #include "../rchol_gb300/csrc/trsv.cu"
+#include "../rchol_gb300/csrc/tree_infer.hpp"
 
 #include <cmath>
 #include <cstdio>
@@ -376,6 +378,12 @@ int main(int argc, char **argv) {
     nodes.push_back({ri[start + total - 1], std::min(ri[start + total], n), depth, false});
   };
   split(0, nr - 1, 1);
+  // "infer": the tree read off G's pattern (as a factor loaded without one gets)
+  const bool infer = argc > 5 && std::string(argv[5]) == "infer";
+  if (infer) {
+    std::vector<int64_t> ci64(ci.begin(), ci.end());
+    nodes = infer_factor_tree(n, rp.data(), ci64.data());
+  }
   // G (CSR of rows) = transpose of the CSR of G^T
   std::vector<int64_t> lrp(n + 1, 0);
   for (int32_t c : ci) lrp[c + 1]++;

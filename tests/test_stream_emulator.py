@@ -37,7 +37,8 @@ def emulator(built):
     os.makedirs(SCRATCH, exist_ok=True)
     exe = os.path.join(SCRATCH, "stream_emulator")
     src = os.path.join(ROOT, "tests", "stream_emulator.cu")
-    deps = [src] + [os.path.join(ROOT, "rchol_gb300", "csrc", f) for f in ("trsv.cu", "plan.hpp", "common.hpp")]
+    deps = [src] + [os.path.join(ROOT, "rchol_gb300", "csrc", f)
+                    for f in ("trsv.cu", "plan.hpp", "common.hpp", "tree_infer.hpp")]
     if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(d) for d in deps):
         subprocess.run([NVCC, "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
                         "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "rchol_gb300", "csrc"),
@@ -97,3 +98,22 @@ def test_emulator_catches_a_misordered_tree(emulator, O):
     bad.tofile(os.path.join(out, "ridx.bin"))
     res = subprocess.run([emulator, out, "2", "0", "1"], capture_output=True, text=True, timeout=300)
     assert res.returncode == 1 and "not yet solved" in res.stdout, res.stdout
+
+
+def test_inferred_tree_is_exact_and_parallel(emulator, factor_dir):
+    """A factor loaded without its tree: the tree read off G's pattern gives
+    streams that read only solved unknowns, solve exactly, and keep most of
+    the parallelism of the ordering's own tree (sequential block steps within
+    1.5x of it, against one chain of n/32 steps without a tree)."""
+    runs = {}
+    for mode in ("tree", "infer"):
+        res = subprocess.run([emulator, factor_dir, "1", "0", "1"] + (["infer"] if mode == "infer" else []),
+                             capture_output=True, text=True, timeout=300)
+        line = res.stdout.strip().splitlines()[-1] if res.stdout.strip() else res.stderr
+        assert res.returncode == 0 and line.startswith("ok"), line
+        runs[mode] = line.split()
+    _, rel_fwd, rel_bwd, _, steps, _ = runs["infer"]
+    assert float(rel_fwd) < 1e-12 and float(rel_bwd) < 1e-12
+    n = int(np.fromfile(os.path.join(factor_dir, "hdr.bin"), np.int64)[0])
+    assert int(steps) <= 1.5 * int(runs["tree"][4]) + 8, (steps, runs["tree"][4])
+    assert int(steps) < 2 * (n + 31) // 32 / 2
