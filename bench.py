@@ -684,8 +684,7 @@ def run_reference(args, rank, world):
         "data": "synthetic (same seeds as the gb300 arm)",
         "config": {"workload": f"PCG to {args.tol:g}, 7-point log-normal Laplacian {args.n}^3, reference rchol G "
                                f"(nnz={len(G[1])}, {args.leaves} subdomains, the gb300 arm's count)",
-                   "grid": args.n, "leaves": args.leaves, "leaves_from": leaves_source, "tol": args.tol,
-            "tuned_launch": {"fp32": knobs32, "fp64": knobs64}, "same_config": True},
+                   "grid": args.n, "leaves": args.leaves, "tol": args.tol, "same_config": True},
         "iters": int(iters), "relres": relres, "relres_host_fp64": ver, "nnz_G": int(len(G[1])),
         "first_solve_s": round(t_first, 1), "order_s": round(t_order, 1), "factor_s": round(t_factor, 1),
         "cpu_baseline": {"value": round(value, 1), "unit": "ms", "cores": threads, "kind": "port",
