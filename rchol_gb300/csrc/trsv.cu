@@ -1372,62 +1372,69 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     int warps;   // pipeline / k-team: warps of the team
     int window;  // warp format: window rows
   };
-  // Per block of [b, e): its rows' entries with columns in [b, e) outside the
-  // block (an upper bound of the record's sparse part, whatever the pieces),
-  // split for the pipeline format into the most entries of one row in the
-  // previous block (n1) and the one before (n2, processing order) and the rest.
-  struct BlockCount {
+  // Pieces grow in processing order (ascending blocks forward, descending
+  // backward).  The record of the block at processing position q of a piece
+  // that starts at position p holds its rows' entries whose columns lie in
+  // positions p..q-1 of the node (entries in earlier pieces are external);
+  // rec_bound is an upper bound of its length in the given format, with the
+  // pipeline format's split by distance (1, 2, more) and `gth` gatherer or
+  // helper threads.
+  struct NodeView {
+    int64_t b, e, nb;
+  };
+  auto rec_bound = [&](const NodeView &v, int fmt, int gth, int64_t q, int64_t p) -> size_t {
+    const int64_t bq = upper ? v.nb - 1 - q : q;
+    const int64_t r0 = v.b + bq * BS, r1 = std::min(v.e, r0 + BS);
+    const size_t csz = v.e - v.b > 65535 ? 4 : 2;
     size_t cnt = 0, far = 0;
     uint32_t n1 = 0, n2 = 0;
-  };
-  auto block_counts = [&](int64_t b, int64_t e) {
-    const int64_t nb = (e - b + BS - 1) / BS;
-    std::vector<BlockCount> cnt(nb);
-    parallel_for(nb, [&](int64_t k0, int64_t k1) {
-      for (int64_t k = k0; k < k1; ++k) {
-        const int64_t r0 = b + k * BS, r1 = std::min(e, r0 + BS);
-        const int64_t b1 = upper ? k + 1 : k - 1, b2 = upper ? k + 2 : k - 2;
-        BlockCount c;
-        for (int64_t i = r0; i < r1; ++i) {
-          uint32_t m1 = 0, m2 = 0;
-          for (int64_t q = rp[i]; q < rp[i + 1]; ++q) {
-            if (ci[q] < b || ci[q] >= e || (ci[q] >= r0 && ci[q] < r1)) continue;
-            ++c.cnt;
-            const int64_t cb = (ci[q] - b) / BS;
-            if (cb == b1) ++m1;
-            else if (cb == b2) ++m2;
-            else ++c.far;
-          }
-          c.n1 = std::max(c.n1, m1);
-          c.n2 = std::max(c.n2, m2);
-        }
-        cnt[k] = c;
+    for (int64_t i = r0; i < r1; ++i) {
+      uint32_t m1 = 0, m2 = 0;
+      for (int64_t t = rp[i]; t < rp[i + 1]; ++t) {
+        const int64_t c = ci[t];
+        if (c < v.b || c >= v.e || (c >= r0 && c < r1)) continue;
+        const int64_t cb = (c - v.b) / BS;
+        const int64_t d = upper ? cb - bq : bq - cb;  // blocks back in processing order
+        if (d > q - p) continue;                      // in an earlier piece: external
+        ++cnt;
+        if (d == 1) ++m1;
+        else if (d == 2) ++m2;
+        else ++far;
       }
-    }, 256);
-    return cnt;
-  };
-  // cut [b, e) into pieces of whole blocks whose shared memory fits:
-  // fixed + nrec * record + rows * row_bytes <= cap (pieces of one node are
-  // solved one after another; entries into earlier pieces become external)
-  auto cut = [&](int64_t b, int64_t e, const std::vector<size_t> &recb, size_t fixed, size_t nrec, size_t row_bytes,
-                 int64_t max_rows, size_t cap, std::vector<std::pair<int64_t, int64_t>> &out) {
-    const int64_t nb = (e - b + BS - 1) / BS;
-    int64_t k = 0;
-    while (k < nb) {
-      int64_t k1 = k;
-      size_t mx = 0;
-      while (k1 < nb) {
-        const size_t m2 = std::max(mx, al16(recb[k1]));
-        const int64_t rows = std::min(e, b + (k1 + 1) * BS) - (b + k * BS);
-        if (k1 > k && (fixed + nrec * m2 + (size_t)rows * row_bytes > cap || rows > max_rows)) break;
-        mx = m2;
-        ++k1;
-      }
-      const int64_t rows = std::min(e, b + k1 * BS) - (b + k * BS);
-      if (fixed + nrec * mx + (size_t)rows * row_bytes > cap) return false;
-      out.push_back({b + k * BS, std::min(e, b + k1 * BS)});
-      k = k1;
+      n1 = std::max(n1, m1);
+      n2 = std::max(n2, m2);
     }
+    if (fmt == FMT_WARP) return w2_record_bound(cnt, vsz, csz);
+    if (fmt == FMT_PIPE) return pipe_record_bound(n1, n2, far, (size_t)gth, vsz, csz);
+    return team_record_bound(cnt, (size_t)gth, vsz, csz);
+  };
+  // Cuts a node into pieces of whole blocks whose shared memory fits:
+  // fixed + nrec * (largest record) + rows * row_bytes <= cap and rows <=
+  // max_rows.  Pieces come back in row order.  False if a single block does
+  // not fit.
+  auto cut = [&](const NodeView &v, int fmt, int gth, size_t fixed, size_t nrec, size_t row_bytes,
+                 int64_t max_rows, size_t cap, std::vector<std::pair<int64_t, int64_t>> &out) {
+    auto rows_of = [&](int64_t p, int64_t q) {  // rows of processing positions [p, q)
+      return upper ? std::min(v.e, v.b + (v.nb - p) * BS) - (v.b + (v.nb - q) * BS)
+                   : std::min(v.e, v.b + q * BS) - (v.b + p * BS);
+    };
+    int64_t p = 0;
+    while (p < v.nb) {
+      int64_t q = p;
+      size_t mx = 0;
+      while (q < v.nb) {
+        const size_t m2 = std::max(mx, al16(rec_bound(v, fmt, gth, q, p)));
+        const int64_t rows = rows_of(p, q + 1);
+        if (q > p && (fixed + nrec * m2 + (size_t)rows * row_bytes > cap || rows > max_rows)) break;
+        mx = m2;
+        ++q;
+      }
+      if (fixed + nrec * mx + (size_t)rows_of(p, q) * row_bytes > cap) return false;
+      if (upper) out.push_back({v.b + (v.nb - q) * BS, std::min(v.e, v.b + (v.nb - p) * BS)});
+      else out.push_back({v.b + p * BS, std::min(v.e, v.b + q * BS)});
+      p = q;
+    }
+    if (upper) std::reverse(out.begin(), out.end());
     return true;
   };
   // longest row-column distance inside [b, e)
@@ -1455,49 +1462,50 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     int fmt = kwidth > 1 ? FMT_KTEAM : fmt_mode == 0 ? FMT_WARP : fmt_mode == 2 ? FMT_PIPE : P >= 2 * sms ? FMT_WARP : FMT_PIPE;
     std::vector<std::vector<Piece>> per_node(P);
     for (int attempt = 0; attempt < 2; ++attempt) {
-      bool ok = true;
-      for (int j = 0; j < P && ok; ++j) {
-        const int64_t b = nodes[j].first, e = nodes[j].second;
-        const std::vector<BlockCount> cnt = block_counts(b, e);
-        std::vector<std::pair<int64_t, int64_t>> rng;
-        per_node[j].clear();
-        if (fmt == FMT_WARP) {
-          std::vector<size_t> recb(cnt.size());
-          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = w2_record_bound(cnt[k].cnt, vsz, e - b > 65535 ? 4 : 2);
-          const int64_t W = std::min<int64_t>(pow2_at_least(std::min<int64_t>(reach_of(b, e) + BS + 1, e - b)),
-                                              kW2WindowMax);
-          const size_t fixed = al16(8 * kW2Ring) + BS * vsz;
-          // rows per piece bounded by the window: a piece of at most W rows
-          // never reads outside it, whatever the node's reach
-          ok = cut(b, e, recb, fixed + (size_t)W * vsz, kW2Ring, 0, W >= kW2WindowMax ? W : INT64_MAX,
-                   kW2WarpBudget, rng);
-          for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_WARP, 1, (int)W});
-        } else if (fmt == FMT_PIPE) {
-          const int warps = pipe_warps_for(P, sms);
-          const int gth = 32 * (warps - 2);
-          std::vector<size_t> recb(cnt.size());
-          for (size_t k = 0; k < cnt.size(); ++k)
-            recb[k] = pipe_record_bound(cnt[k].n1, cnt[k].n2, cnt[k].far, gth, vsz, e - b > 65535 ? 4 : 2);
-          const size_t fixed = al16(8 * 8) + al16(vsz * (3 * BS + 2 * (size_t)gth));
-          // the ring the pieces are cut for; the smallest one (4) where even a
-          // single block's records would not fit a deeper ring
-          ok = cut(b, e, recb, fixed, kPipeRingCut, vsz, 1 << 30, kSmemCap, rng);
-          if (!ok) {
-            rng.clear();
-            ok = cut(b, e, recb, fixed, 4, vsz, 1 << 30, kSmemCap, rng);
+      std::vector<char> node_ok(P, 1);
+      parallel_for(P, [&](int64_t j0, int64_t j1) {
+        for (int64_t j = j0; j < j1; ++j) {
+          const NodeView v{nodes[j].first, nodes[j].second, (nodes[j].second - nodes[j].first + BS - 1) / BS};
+          std::vector<std::pair<int64_t, int64_t>> rng;
+          per_node[j].clear();
+          bool ok;
+          if (fmt == FMT_WARP) {
+            const int64_t W = std::min<int64_t>(pow2_at_least(std::min<int64_t>(reach_of(v.b, v.e) + BS + 1, v.e - v.b)),
+                                                kW2WindowMax);
+            const size_t fixed = al16(8 * kW2Ring) + BS * vsz + (size_t)W * vsz;
+            // rows per piece bounded by the window: a piece of at most W rows
+            // never reads outside it, whatever the node's reach
+            ok = cut(v, fmt, 0, fixed, kW2Ring, 0, W >= kW2WindowMax ? W : INT64_MAX, kW2WarpBudget, rng);
+            for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_WARP, 1, (int)W});
+          } else if (fmt == FMT_PIPE) {
+            const int warps = pipe_warps_for(P, sms);
+            const int gth = 32 * (warps - 2);
+            const size_t fixed = al16(8 * 8) + al16(vsz * (3 * BS + 2 * (size_t)gth));
+            // the ring the pieces are cut for, the smallest one (4) where a
+            // single block's record would not fit a deeper one
+            ok = cut(v, fmt, gth, fixed, kPipeRingCut, vsz, 1 << 30, kSmemCap, rng);
+            if (!ok) {
+              rng.clear();
+              ok = cut(v, fmt, gth, fixed, 4, vsz, 1 << 30, kSmemCap, rng);
+            }
+            for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_PIPE, warps, 0});
+          } else {
+            const int warps = 8, hth = 32 * (warps - 1);
+            const size_t fixed = 2 * (size_t)BS * KW * vsz;
+            ok = cut(v, fmt, hth, fixed, TEAM_RING, vsz * KW, 65535, kSmemCap, rng);
+            for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_KTEAM, warps, 0});
           }
-          for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_PIPE, warps, 0});
-        } else {
-          const int warps = 8, hth = 32 * (warps - 1);
-          std::vector<size_t> recb(cnt.size());
-          for (size_t k = 0; k < cnt.size(); ++k) recb[k] = team_record_bound(cnt[k].cnt, hth, vsz, e - b > 65535 ? 4 : 2);
-          const size_t fixed = 2 * (size_t)BS * KW * vsz;
-          ok = cut(b, e, recb, fixed, TEAM_RING, vsz * KW, 65535, kSmemCap, rng);
-          for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_KTEAM, warps, 0});
+          node_ok[j] = ok;
         }
-      }
-      if (ok) break;
-      if (fmt != FMT_WARP) throw Error(RCHOL_ERR_INTERNAL, "a 32-row block of G is too dense for the shared-memory solve");
+      }, 1);
+      int bad = -1;
+      for (int j = 0; j < P && bad < 0; ++j)
+        if (!node_ok[j]) bad = j;
+      if (bad < 0) break;
+      if (fmt != FMT_WARP)
+        throw Error(RCHOL_ERR_INTERNAL, "a 32-row block of G is too dense for the shared-memory solve (depth " +
+                                            std::to_string(depth) + ", node rows " + std::to_string(nodes[bad].first) +
+                                            ".." + std::to_string(nodes[bad].second) + ")");
       fmt = FMT_PIPE;  // records too large for a warp's share: this depth in the pipeline format
     }
     std::vector<std::vector<Piece>> by_index;  // piece j of every node of this depth

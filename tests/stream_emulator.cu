@@ -418,6 +418,32 @@ int main(int argc, char **argv) {
   HostStreamCopy Hf, Hb;
   build_dir_streams(lrp, lci, lv, n, nodes, false, fp32, team_mode, kwidth, Df, 0, &Hf);
   build_dir_streams(rp, ci, v, n, nodes, true, fp32, team_mode, kwidth, Db, 0, &Hb);
+  if (argc > 5 && std::string(argv[5]) == "stats") {  // the plan only: one line per stage
+    for (int dir = 0; dir < 2; ++dir) {
+      const StreamDir &D = dir ? Db : Df;
+      const HostStreamCopy &H = dir ? Hb : Hf;
+      std::printf("%s: %zu stages, %lld block steps, %lld record bytes\n", dir ? "backward" : "forward",
+                  D.stage_ptr.size() - 1, (long long)D.steps, (long long)H.blocks.size());
+      for (size_t st = 0; st + 1 < D.stage_ptr.size(); ++st) {
+        int64_t rows = 0, blocks = 0, bytes = 0, ext = 0;
+        int maxnb = 0;
+        for (int k = D.stage_ptr[st]; k < D.stage_ptr[st + 1]; ++k) {
+          const NodeDesc &nd = H.desc[k];
+          rows += nd.rows;
+          blocks += nd.nblocks;
+          maxnb = std::max(maxnb, nd.nblocks);
+          bytes += H.blk_off[nd.blk0 + nd.nblocks] - H.blk_off[nd.blk0];
+          ext += H.ext_rp[nd.begin + nd.rows] - H.ext_rp[nd.begin];
+        }
+        std::printf("  st %2zu fmt %d pieces %5d rows %9lld maxrows %6d steps %5d maxrec %6d win %5d warps %2d "
+                    "chunks %4d recMB %8.1f ext %10lld\n",
+                    st, D.stage_fmt[st], D.stage_ptr[st + 1] - D.stage_ptr[st], (long long)rows, D.stage_rows[st],
+                    maxnb, D.stage_maxrec[st], D.stage_window[st], D.stage_warps[st], D.stage_chunks[st],
+                    bytes / 1e6, (long long)ext);
+      }
+    }
+    return 0;
+  }
   long tf = 0, tb = 0, wf = 0, wb = 0;
   const auto ye = fp32 ? emulate<float>(Hf, b, n, false, tf, wf) : emulate<double>(Hf, b, n, false, tf, wf);
   const auto ze = fp32 ? emulate<float>(Hb, y, n, true, tb, wb) : emulate<double>(Hb, y, n, true, tb, wb);
