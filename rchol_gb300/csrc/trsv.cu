@@ -1034,9 +1034,131 @@ __device__ __forceinline__ VT apply_row(const VT (&m)[BS], const VT *tb) {
   return (a0 + a1) + (a2 + a3);
 }
 
+// Sparse dot products of one lane's row, eight entries at a time: the
+// column and value loads of a batch are issued together, then the gathers of
+// the solved values, then the FMAs (a dependent load-gather-FMA chain per
+// entry would cost a shared-memory round trip each).
+
+// slot-major entries: entry j of the lane's row at j * 32 + lane; columns
+// relative to `base`
+template <typename VT>
+__device__ __forceinline__ VT slot_dot(const unsigned char *col, const VT *val, const VT *x, uint32_t base,
+                                       uint32_t cnt, int lane) {
+  VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  for (uint32_t j0 = 0; j0 < cnt; j0 += 8) {
+    uint32_t c[8];
+    VT v[8], g[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool ok = j0 + u < cnt;
+      c[u] = ok ? (uint32_t)col[(j0 + u) * BS + lane] : 0u;
+      v[u] = ok ? val[(j0 + u) * BS + lane] : VT(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) g[u] = x[base + c[u]];
+#pragma unroll
+    for (int u = 0; u < 8; u += 4) {
+      a0 = fma(v[u], g[u], a0);
+      a1 = fma(v[u + 1], g[u + 1], a1);
+      a2 = fma(v[u + 2], g[u + 2], a2);
+      a3 = fma(v[u + 3], g[u + 3], a3);
+    }
+  }
+  return (a0 + a1) + (a2 + a3);
+}
+
+// contiguous entries [e0, e1) with piece-local columns, solved values at x[col & wmask]
+template <typename VT, typename CT>
+__device__ __forceinline__ VT run_dot(const CT *col, const VT *val, const VT *x, uint32_t wmask, uint32_t e0,
+                                      uint32_t e1) {
+  VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  for (uint32_t e = e0; e < e1; e += 8) {
+    uint32_t c[8];
+    VT v[8], g[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool ok = e + u < e1;
+      c[u] = ok ? (uint32_t)col[e + u] : 0u;
+      v[u] = ok ? val[e + u] : VT(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) g[u] = x[c[u] & wmask];
+#pragma unroll
+    for (int u = 0; u < 8; u += 4) {
+      a0 = fma(v[u], g[u], a0);
+      a1 = fma(v[u + 1], g[u + 1], a1);
+      a2 = fma(v[u + 2], g[u + 2], a2);
+      a3 = fma(v[u + 3], g[u + 3], a3);
+    }
+  }
+  return (a0 + a1) + (a2 + a3);
+}
+
+// sum of p[c0 .. c1)
+template <typename VT>
+__device__ __forceinline__ VT range_sum(const VT *p, uint32_t c0, uint32_t c1) {
+  VT a0 = 0, a1 = 0;
+  for (uint32_t c = c0; c < c1; c += 8) {
+    VT v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = c + u < c1 ? p[c + u] : VT(0);
+#pragma unroll
+    for (int u = 0; u < 8; u += 2) {
+      a0 += v[u];
+      a1 += v[u + 1];
+    }
+  }
+  return a0 + a1;
+}
+
+// chunk g of `nchunk` interleaved chunks of `clen` entries (entry j at j * nchunk + g)
+template <typename VT, typename CT>
+__device__ __forceinline__ VT chunk_dot(const CT *col, const VT *val, const VT *x, uint32_t g, uint32_t nchunk,
+                                        uint32_t clen) {
+  VT a0 = 0, a1 = 0;
+  for (uint32_t j0 = 0; j0 < clen; j0 += 4) {
+    uint32_t c[4];
+    VT v[4], xv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const bool ok = j0 + u < clen;
+      const uint32_t at = (j0 + u) * nchunk + g;
+      c[u] = ok ? (uint32_t)col[at] : 0u;
+      v[u] = ok ? val[at] : VT(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) xv[u] = x[c[u]];
+    a0 = fma(v[0], xv[0], a0);
+    a1 = fma(v[1], xv[1], a1);
+    a0 = fma(v[2], xv[2], a0);
+    a1 = fma(v[3], xv[3], a1);
+  }
+  return a0 + a1;
+}
+
 template <typename VT, typename InT>
 __device__ __forceinline__ VT rhs_at(const VT *acc, const InT *in, int64_t i) {
   return acc ? __ldg(acc + i) : (VT)__ldg(in + i);
+}
+
+// Position of a record in a ring of mbarrier-guarded slots: record k sits in
+// slot k mod R and completes phase k / R of that slot's barrier; each role
+// walks its records in order, so the position advances by one per record.
+struct RingPos {
+  int slot = 0;
+  uint32_t par = 0;
+  __device__ __forceinline__ void next(int R) {
+    if (++slot == R) {
+      slot = 0;
+      par ^= 1u;
+    }
+  }
+};
+
+template <int SZ>
+__device__ __forceinline__ void cp_async_small(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(SZ) : "memory");
 }
 
 template <typename VT>
@@ -1044,7 +1166,7 @@ struct W2Args {
   const NodeDesc *nodes;
   int node0, node1;   // pieces of this stage
   int wpb;            // warps (pieces) per thread block
-  int nbuf;           // ring slots per warp
+  int nbuf;           // record slots per warp
   int bufbytes;       // bytes of a slot (16-aligned)
   int per_warp;       // shared-memory bytes per warp (16-aligned)
   int pf;             // records prefetched into L2 ahead of use (0: none)
@@ -1054,8 +1176,19 @@ struct W2Args {
   const VT *acc;      // rhs minus external sums, or null: the stage reads `in`
 };
 
+constexpr int kW2RhsRing = 4;  // warp format: blocks of right-hand side in flight per warp (a power of two)
+
+// Shared memory of one warp of w2_kernel.
+template <typename VT>
+__host__ __device__ inline size_t w2_warp_bytes(int nbuf, size_t bufbytes, size_t window) {
+  return al16(al16(8 * (size_t)nbuf) + BS * sizeof(VT) + (size_t)kW2RhsRing * BS * 8 + (size_t)nbuf * bufbytes +
+              window * sizeof(VT));
+}
+
 // One warp per piece; per-warp shared memory: mbarriers, the broadcast
-// buffer of t, the record ring, the window of solved values.
+// buffer of t, the right-hand-side ring, the record ring, the window of
+// solved values.  The right-hand side of block k+3 streams in with per-lane
+// cp.async while block k is solved, so no register waits on a global load.
 template <typename VT, typename InT, typename OutT, bool UPPER>
 __global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__restrict__ in, OutT *__restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1067,7 +1200,8 @@ __global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__rest
   unsigned char *base = smem + (size_t)w * a.per_warp;
   uint64_t *bar = reinterpret_cast<uint64_t *>(base);
   VT *tsh = reinterpret_cast<VT *>(base + al16(8 * (size_t)NB));
-  unsigned char *ring = reinterpret_cast<unsigned char *>(tsh + BS);
+  double *rq = reinterpret_cast<double *>(tsh + BS);  // [kW2RhsRing][32] raw right-hand sides, 8-byte slots
+  unsigned char *ring = reinterpret_cast<unsigned char *>(rq + kW2RhsRing * BS);
   VT *xw = reinterpret_cast<VT *>(ring + (size_t)NB * a.bufbytes);
   const uint32_t wmask = a.wmask;
   OffCache oc;
@@ -1077,23 +1211,37 @@ __global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__rest
     fence_mbar_init();
   }
   __syncwarp();
-  auto issue = [&](int k) {  // all lanes (offset shuffles); lane 0 copies record k into slot k % NB
+  auto issue = [&](int k, int slot) {  // all lanes (offset shuffles); lane 0 copies record k
     const int64_t o0 = oc.get(k), o1 = oc.get(k + 1);
-    if (lane == 0) bulk_load(ring + (size_t)(k % NB) * a.bufbytes, a.blocks + o0, (uint32_t)(o1 - o0), bar + k % NB);
+    if (lane == 0) bulk_load(ring + (size_t)slot * a.bufbytes, a.blocks + o0, (uint32_t)(o1 - o0), bar + slot);
   };
-  for (int k = 0; k < NB && k < nb; ++k) issue(k);
-  auto rhs = [&](int k) -> VT {  // right-hand side of row `lane` of block k
-    const int row = (UPPER ? nb - 1 - k : k) * BS + lane;
-    return (k < nb && row < nd.rows) ? rhs_at(a.acc, in, nd.begin + row) : VT(0);
+  for (int k = 0; k < NB && k < nb; ++k) issue(k, k);
+  auto fetch_rhs = [&](int k) {  // row `lane` of block k into its ring slot; one commit group per block
+    if (k < nb) {
+      const int row = (UPPER ? nb - 1 - k : k) * BS + lane;
+      if (row < nd.rows) {
+        void *dst = rq + (k & (kW2RhsRing - 1)) * BS + lane;
+        if (a.acc) {
+          if (sizeof(VT) == 8) cp_async_small<8>(dst, a.acc + nd.begin + row);
+          else cp_async_small<4>(dst, a.acc + nd.begin + row);
+        } else {
+          if (sizeof(InT) == 8) cp_async_small<8>(dst, in + nd.begin + row);
+          else cp_async_small<4>(dst, in + nd.begin + row);
+        }
+      }
+    }
+    cp_async_commit();
   };
-  VT q0 = rhs(0), q1 = rhs(1), q2 = rhs(2);
+  for (int k = 0; k < kW2RhsRing - 1; ++k) fetch_rhs(k);
+  RingPos pos;
   int k = 0;
   bool ok = true;
   for (; k < nb; ++k) {
-    const int slot = k % NB;
-    ok = __all_sync(0xffffffffu, mbar_wait(bar + slot, (uint32_t)(k / NB) & 1u));
+    fetch_rhs(k + kW2RhsRing - 1);
+    ok = __all_sync(0xffffffffu, mbar_wait(bar + pos.slot, pos.par));
     if (!ok) break;
-    const unsigned char *p = ring + (size_t)slot * a.bufbytes;
+    cp_async_wait<kW2RhsRing - 1>();  // block k's right-hand side (this lane's own copy) is in
+    const unsigned char *p = ring + (size_t)pos.slot * a.bufbytes;
     const uint4 h = *reinterpret_cast<const uint4 *>(p);
     const uint32_t nr = h.x, row0 = h.y, nent = h.z, csz = h.w;
     const W2Layout L = w2_layout(nent, csz, sizeof(VT));
@@ -1101,52 +1249,39 @@ __global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__rest
     load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + L.o_tinv), lane, m);
     const uint16_t *eoff = reinterpret_cast<const uint16_t *>(p + L.o_eoff);
     const VT *val = reinterpret_cast<const VT *>(p + L.o_val);
-    uint32_t e = eoff[lane];
-    const uint32_t e1 = eoff[lane + 1];
-    VT s0 = 0, s1 = 0;
-    if (csz == 2) {
-      const uint16_t *col = reinterpret_cast<const uint16_t *>(p + L.o_col);
-      for (; e + 1 < e1; e += 2) {
-        s0 = fma(val[e], xw[col[e] & wmask], s0);
-        s1 = fma(val[e + 1], xw[col[e + 1] & wmask], s1);
-      }
-      if (e < e1) s0 = fma(val[e], xw[col[e] & wmask], s0);
-    } else {
-      const uint32_t *col = reinterpret_cast<const uint32_t *>(p + L.o_col);
-      for (; e + 1 < e1; e += 2) {
-        s0 = fma(val[e], xw[col[e] & wmask], s0);
-        s1 = fma(val[e + 1], xw[col[e + 1] & wmask], s1);
-      }
-      if (e < e1) s0 = fma(val[e], xw[col[e] & wmask], s0);
-    }
-    tsh[lane] = lane < (int)nr ? q0 - (s0 + s1) : VT(0);
+    const uint32_t e0 = eoff[lane], e1 = eoff[lane + 1];
+    const VT sum = csz == 2 ? run_dot(reinterpret_cast<const uint16_t *>(p + L.o_col), val, xw, wmask, e0, e1)
+                            : run_dot(reinterpret_cast<const uint32_t *>(p + L.o_col), val, xw, wmask, e0, e1);
+    const void *rp = rq + (k & (kW2RhsRing - 1)) * BS + lane;
+    const VT q0 = a.acc ? *reinterpret_cast<const VT *>(rp) : (VT) * reinterpret_cast<const InT *>(rp);
+    tsh[lane] = lane < (int)nr ? q0 - sum : VT(0);
     __syncwarp();
     const VT x = apply_row(m, tsh);
     if (lane < (int)nr) {
       xw[(row0 + lane) & wmask] = x;
       out[nd.begin + row0 + lane] = (OutT)x;
     }
-    q0 = q1;
-    q1 = q2;
-    q2 = rhs(k + 3);
     __syncwarp();  // slot and tsh free again
     oc.advance(k + NB, lane);  // the lowest record index used below
     if (k + NB < nb) {
       if (lane == 0) fence_proxy_async();
-      issue(k + NB);
+      issue(k + NB, pos.slot);
     }
     if (a.pf && k + a.pf < nb) {
       const int64_t o0 = oc.get(k + a.pf), o1 = oc.get(k + a.pf + 1);
       if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
     }
+    pos.next(NB);
   }
   if (!ok) {  // give up: wait (bounded) for the copies still in flight, one per slot
     if (lane == 0) {
       atomicOr(&g_solve_status, 1u);
-      for (int j = k; j < nb && j < k + NB; ++j) (void)mbar_wait(bar + j % NB, (uint32_t)(j / NB) & 1u);
+      RingPos q = pos;
+      for (int j = k; j < nb && j < k + NB; ++j, q.next(NB)) (void)mbar_wait(bar + q.slot, q.par);
     }
     __syncwarp();
   }
+  cp_async_wait<0>();
 }
 
 template <typename VT>
@@ -1162,13 +1297,29 @@ struct PipeArgs {
   const VT *acc;     // rhs minus external sums, or null: the stage reads `in`
 };
 
-// One thread block per piece: warp 0 solves, warp 1 reduces and streams the
-// records, warps 2.. gather.  One __syncthreads per step; in step s the
-// solver retires block s, the reducer prepares u for block s+1, the
-// gatherers sum the far entries of block s+2.  The piece's right-hand side
-// and then its solution live in shared memory (xs).
+// distance-1 entries per row the solver loads before the step's barrier
+// (fewer for FP64, whose inverse row already takes 64 registers)
+template <typename VT>
+__host__ __device__ constexpr int pipe_pre() {
+  return sizeof(VT) == 4 ? 8 : 4;
+}
+
+// One thread block per piece: warp 0 solves, warp 1 reduces, warps 2..
+// gather, warp 2 also streams the records.  One __syncthreads per step; in
+// step s the solver retires block s, the reducer prepares u for block s+1,
+// the gatherers sum the far entries of block s+2.  Everything of block s+1
+// that does not depend on block s -- its header, inverse row and first
+// distance-1 entries -- the solver loads before the barrier.  The piece's
+// right-hand side and then its solution live in shared memory (xs).
+// FP64 teams have at most 12 warps (170 registers a thread: the inverse row
+// alone takes 64)
+template <typename VT>
+__host__ __device__ constexpr int pipe_max_threads() {
+  return sizeof(VT) == 8 ? 384 : 512;
+}
+
 template <typename VT, typename InT, typename OutT, bool UPPER>
-__global__ void __launch_bounds__(512, 1) pipe_kernel(PipeArgs<VT> a, const InT *__restrict__ in,
+__global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArgs<VT> a, const InT *__restrict__ in,
                                                       OutT *__restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int abort_flag;
@@ -1182,141 +1333,163 @@ __global__ void __launch_bounds__(512, 1) pipe_kernel(PipeArgs<VT> a, const InT 
   unsigned char *ring = reinterpret_cast<unsigned char *>(tsh) + al16(sizeof(VT) * (3 * BS + 2 * (size_t)a.maxchunk));
   VT *xs = reinterpret_cast<VT *>(ring + (size_t)RING * a.bufbytes);
   OffCache oc;
-  if (warp == 1) oc.init(a.blk_off + nd.blk0, nb, lane);
+  if (warp == 2) oc.init(a.blk_off + nd.blk0, nb, lane);
   if (tid == 0) {
     abort_flag = 0;
     for (int i = 0; i < RING; ++i) mbar_init(bar + i, 1);
     fence_mbar_init();
   }
-  for (int r = tid; r < nd.rows; r += blockDim.x) xs[r] = rhs_at(a.acc, in, nd.begin + r);
+  // the piece's right-hand side into shared memory, eight loads in flight per thread
+  for (int r0 = tid; r0 < nd.rows; r0 += 8 * (int)blockDim.x) {
+    VT v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int r = r0 + u * (int)blockDim.x;
+      v[u] = r < nd.rows ? rhs_at(a.acc, in, nd.begin + r) : VT(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int r = r0 + u * (int)blockDim.x;
+      if (r < nd.rows) xs[r] = v[u];
+    }
+  }
   __syncthreads();
-  auto slot_of = [&](int k) { return ring + (size_t)(k % RING) * a.bufbytes; };
-  auto issue = [&](int k) {  // warp 1: record k into its slot
+  auto slot_ptr = [&](int slot) { return ring + (size_t)slot * a.bufbytes; };
+  RingPos ld;  // warp 2: slot of the next record to issue
+  uint32_t issued = 0;
+  auto issue = [&](int k) {  // warp 2: record k into the next slot
     const int64_t o0 = oc.get(k), o1 = oc.get(k + 1);
-    if (lane == 0) bulk_load(slot_of(k), a.blocks + o0, (uint32_t)(o1 - o0), bar + k % RING);
+    if (lane == 0) bulk_load(slot_ptr(ld.slot), a.blocks + o0, (uint32_t)(o1 - o0), bar + ld.slot);
+    ld.next(RING);
+    issued = (uint32_t)(k + 1);
   };
-  if (warp == 1)
+  if (warp == 2)
     for (int k = 0; k < RING - 3 && k < nb; ++k) issue(k);
-  auto wait_rec = [&](int k) {
-    if (!mbar_wait(bar + k % RING, (uint32_t)(k / RING) & 1u)) {
+  auto wait_at = [&](const RingPos &q) {
+    if (!mbar_wait(bar + q.slot, q.par)) {
       atomicOr(&g_solve_status, 1u);
       abort_flag = 1;
       return false;
     }
     return true;
   };
-  VT m[BS];  // solver: inverse row of its next block
-  uint32_t issued = (uint32_t)min(RING - 3, nb);
+  RingPos pos;  // the next record this thread's role reads
+  // solver: block s+1 loaded ahead of the barrier
+  VT m[BS];
+  constexpr int kPipePre = pipe_pre<VT>();
+  uint32_t s_nr = 0, s_row0 = 0, s_prow0 = 0, s_n1 = 0, pc[kPipePre];
+  VT pv[kPipePre];
+  const unsigned char *s_n1c = nullptr;
+  const VT *s_n1v = nullptr;
   for (int s = -2; s < nb; ++s) {
     const bool stop = abort_flag != 0;  // read after the last barrier: uniform
     if (!stop) {
       if (warp == 0) {
         if (s >= 0) {
-          const unsigned char *p = slot_of(s);
-          const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
-          const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
-          const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
-          const uint32_t nr = h0.x, row0 = h0.y, prow0 = h0.z, n1 = h1.x;
-          const unsigned char *n1c = p + h2.y;
-          const VT *n1v = reinterpret_cast<const VT *>(p + h2.z);
-          VT t0 = lane < (int)nr ? ubuf[(s & 1) * BS + lane] : VT(0), t1 = 0;
-          uint32_t j = 0;
-          for (; j + 1 < n1; j += 2) {
-            t0 = fma(-n1v[j * BS + lane], xs[prow0 + n1c[j * BS + lane]], t0);
-            t1 = fma(-n1v[(j + 1) * BS + lane], xs[prow0 + n1c[(j + 1) * BS + lane]], t1);
+          VT g[kPipePre];
+#pragma unroll
+          for (int u = 0; u < kPipePre; ++u) g[u] = xs[s_prow0 + pc[u]];
+          VT a0 = 0, a1 = 0;
+#pragma unroll
+          for (int u = 0; u < kPipePre; u += 2) {
+            a0 = fma(pv[u], g[u], a0);
+            a1 = fma(pv[u + 1], g[u + 1], a1);
           }
-          if (j < n1) t0 = fma(-n1v[j * BS + lane], xs[prow0 + n1c[j * BS + lane]], t0);
-          tsh[lane] = lane < (int)nr ? t0 + t1 : VT(0);
+          VT near = a0 + a1;
+          if (s_n1 > (uint32_t)kPipePre)
+            near += slot_dot(s_n1c + kPipePre * BS, s_n1v + kPipePre * BS, xs, s_prow0, s_n1 - kPipePre, lane);
+          const VT u = lane < (int)s_nr ? ubuf[(s & 1) * BS + lane] : VT(0);
+          tsh[lane] = lane < (int)s_nr ? u - near : VT(0);
           __syncwarp();
           const VT x = apply_row(m, tsh);
-          if (lane < (int)nr) {
-            xs[row0 + lane] = x;
-            out[nd.begin + row0 + lane] = (OutT)x;
+          if (lane < (int)s_nr) {
+            xs[s_row0 + lane] = x;
+            out[nd.begin + s_row0 + lane] = (OutT)x;
           }
         }
-        if (s + 1 >= 0 && s + 1 < nb) {  // next block's inverse row, ahead of the barrier
-          if (wait_rec(s + 1)) load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(slot_of(s + 1) + 64), lane, m);
+        if (s + 1 >= 0 && s + 1 < nb) {  // block s+1: everything that does not depend on block s
+          if (wait_at(pos)) {
+            const unsigned char *p = slot_ptr(pos.slot);
+            const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
+            const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
+            const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
+            s_nr = h0.x;
+            s_row0 = h0.y;
+            s_prow0 = h0.z;
+            s_n1 = h1.x;
+            s_n1c = p + h2.y;
+            s_n1v = reinterpret_cast<const VT *>(p + h2.z);
+            load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + 64), lane, m);
+#pragma unroll
+            for (int u = 0; u < kPipePre; ++u) {
+              const bool ok = (uint32_t)u < s_n1;
+              pc[u] = ok ? (uint32_t)s_n1c[u * BS + lane] : 0u;
+              pv[u] = ok ? -s_n1v[u * BS + lane] : VT(0);
+            }
+          }
+          pos.next(RING);
         }
       } else if (warp == 1) {
-        // stream: record s-1+RING into the slot of record s-1 (retired last step)
-        const int k = s - 1 + RING;
-        oc.advance(a.pf ? min(k, s + a.pf) : k, lane);  // the lowest record index used this step
-        if (k >= RING - 3 && k < nb) {
-          if (lane == 0) fence_proxy_async();
-          issue(k);
-          issued = (uint32_t)(k + 1);
-        }
-        if (a.pf && s + a.pf >= 0 && s + a.pf < nb) {
-          const int64_t o0 = oc.get(s + a.pf), o1 = oc.get(s + a.pf + 1);
-          if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
-        }
         const int bk = s + 1;  // reducer: u of block s+1
-        if (bk >= 0 && bk < nb && wait_rec(bk)) {
-          const unsigned char *p = slot_of(bk);
-          const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
-          const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
-          const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
-          const uint4 h3 = *reinterpret_cast<const uint4 *>(p + 48);
-          const uint32_t nr = h0.x, row0 = h0.y, pprow0 = h0.w, n2 = h1.y;
-          const unsigned char *n2c = p + h2.w;
-          const VT *n2v = reinterpret_cast<const VT *>(p + h3.x);
-          const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h3.y);
-          const VT *pb = part + (size_t)(bk & 1) * a.maxchunk;
-          VT u0 = lane < (int)nr ? xs[row0 + lane] : VT(0), u1 = 0;
-          uint32_t c = crow[lane];
-          const uint32_t c1 = crow[lane + 1];
-          for (; c + 1 < c1; c += 2) {
-            u0 -= pb[c];
-            u1 -= pb[c + 1];
+        if (bk >= 0 && bk < nb) {
+          if (wait_at(pos)) {
+            const unsigned char *p = slot_ptr(pos.slot);
+            const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
+            const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
+            const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
+            const uint4 h3 = *reinterpret_cast<const uint4 *>(p + 48);
+            const uint32_t nr = h0.x, row0 = h0.y, pprow0 = h0.w, n2 = h1.y;
+            const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h3.y);
+            const VT *pb = part + (size_t)(bk & 1) * a.maxchunk;
+            const VT acc0 = lane < (int)nr ? xs[row0 + lane] : VT(0);
+            const VT far = range_sum(pb, crow[lane], crow[lane + 1]);
+            const VT mid = slot_dot(p + h2.w, reinterpret_cast<const VT *>(p + h3.x), xs, pprow0, n2, lane);
+            ubuf[(bk & 1) * BS + lane] = lane < (int)nr ? acc0 - (far + mid) : VT(0);
           }
-          if (c < c1) u0 -= pb[c];
-          uint32_t j = 0;
-          for (; j + 1 < n2; j += 2) {
-            u0 = fma(-n2v[j * BS + lane], xs[pprow0 + n2c[j * BS + lane]], u0);
-            u1 = fma(-n2v[(j + 1) * BS + lane], xs[pprow0 + n2c[(j + 1) * BS + lane]], u1);
-          }
-          if (j < n2) u0 = fma(-n2v[j * BS + lane], xs[pprow0 + n2c[j * BS + lane]], u0);
-          ubuf[(bk & 1) * BS + lane] = lane < (int)nr ? u0 + u1 : VT(0);
+          pos.next(RING);
         }
       } else {
-        const int bk = s + 2;  // gatherers: far sums of block s+2
-        if (bk < nb && wait_rec(bk)) {
-          const unsigned char *p = slot_of(bk);
-          const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
-          const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
-          const uint4 h3 = *reinterpret_cast<const uint4 *>(p + 48);
-          const uint32_t nchunk = h1.z, clen = h1.w, csz = h2.x;
-          const int g = tid - 64;
-          if (g < (int)nchunk) {
-            const VT *fv = reinterpret_cast<const VT *>(p + h3.w);
-            VT s0 = 0, s1 = 0;
-            uint32_t jj = 0, at = (uint32_t)g;
-            if (csz == 2) {
-              const uint16_t *fc = reinterpret_cast<const uint16_t *>(p + h3.z);
-              for (; jj + 1 < clen; jj += 2, at += 2 * nchunk) {
-                s0 = fma(fv[at], xs[fc[at]], s0);
-                s1 = fma(fv[at + nchunk], xs[fc[at + nchunk]], s1);
-              }
-              if (jj < clen) s0 = fma(fv[at], xs[fc[at]], s0);
-            } else {
-              const uint32_t *fc = reinterpret_cast<const uint32_t *>(p + h3.z);
-              for (; jj + 1 < clen; jj += 2, at += 2 * nchunk) {
-                s0 = fma(fv[at], xs[fc[at]], s0);
-                s1 = fma(fv[at + nchunk], xs[fc[at + nchunk]], s1);
-              }
-              if (jj < clen) s0 = fma(fv[at], xs[fc[at]], s0);
-            }
-            part[(size_t)(bk & 1) * a.maxchunk + g] = s0 + s1;
+        if (warp == 2) {  // stream record s-1+RING into the slot of record s-1 (retired last step)
+          const int k = s - 1 + RING;
+          oc.advance(a.pf ? min(k, s + a.pf) : k, lane);  // the lowest record index used this step
+          if (k >= RING - 3 && k < nb) {
+            if (lane == 0) fence_proxy_async();
+            issue(k);
           }
+          if (a.pf && s + a.pf >= 0 && s + a.pf < nb) {
+            const int64_t o0 = oc.get(s + a.pf), o1 = oc.get(s + a.pf + 1);
+            if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
+          }
+        }
+        const int bk = s + 2;  // gatherers: far sums of block s+2
+        if (bk < nb) {
+          if (wait_at(pos)) {
+            const unsigned char *p = slot_ptr(pos.slot);
+            const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
+            const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
+            const uint4 h3 = *reinterpret_cast<const uint4 *>(p + 48);
+            const uint32_t nchunk = h1.z, clen = h1.w, csz = h2.x;
+            const int g = tid - 64;
+            if (g < (int)nchunk) {
+              const VT *fv = reinterpret_cast<const VT *>(p + h3.w);
+              part[(size_t)(bk & 1) * a.maxchunk + g] =
+                  csz == 2 ? chunk_dot(reinterpret_cast<const uint16_t *>(p + h3.z), fv, xs, (uint32_t)g, nchunk, clen)
+                           : chunk_dot(reinterpret_cast<const uint32_t *>(p + h3.z), fv, xs, (uint32_t)g, nchunk, clen);
+            }
+          }
+          pos.next(RING);
         }
       }
     }
     __syncthreads();
   }
-  if (abort_flag && warp == 1 && lane == 0) {
+  if (abort_flag && warp == 2 && lane == 0) {
     // copies that may still be in flight: the last RING issued, one per slot
-    for (int j = max(0, (int)issued - RING); j < (int)issued; ++j)
-      (void)mbar_wait(bar + j % RING, (uint32_t)(j / RING) & 1u);
+    RingPos q;
+    for (int j = 0; j < (int)issued; ++j) {
+      if (j >= (int)issued - RING) (void)mbar_wait(bar + q.slot, q.par);
+      q.next(RING);
+    }
   }
 }
 
@@ -1356,7 +1529,9 @@ constexpr int kPipeRingCut = 6;              // pipeline format: ring the pieces
 
 // Pipeline team size of a stage with `pieces` pieces: 16 warps where at
 // most one piece runs per SM, fewer (several teams per SM) beyond.
-static int pipe_warps_for(int pieces, int sms) { return pieces <= sms ? 16 : pieces <= 2 * sms ? 8 : 4; }
+static int pipe_warps_for(int pieces, int sms, size_t vsz) {
+  return pieces <= sms ? (vsz == 8 ? 12 : 16) : pieces <= 2 * sms ? 8 : 4;
+}
 
 static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
                               const std::vector<double> &v, int64_t n, const std::vector<TreeNode> &tnodes,
@@ -1472,13 +1647,13 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
           if (fmt == FMT_WARP) {
             const int64_t W = std::min<int64_t>(pow2_at_least(std::min<int64_t>(reach_of(v.b, v.e) + BS + 1, v.e - v.b)),
                                                 kW2WindowMax);
-            const size_t fixed = al16(8 * kW2Ring) + BS * vsz + (size_t)W * vsz;
+            const size_t fixed = al16(8 * kW2Ring) + BS * vsz + (size_t)kW2RhsRing * BS * 8 + (size_t)W * vsz;
             // rows per piece bounded by the window: a piece of at most W rows
             // never reads outside it, whatever the node's reach
             ok = cut(v, fmt, 0, fixed, kW2Ring, 0, W >= kW2WindowMax ? W : INT64_MAX, kW2WarpBudget, rng);
             for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_WARP, 1, (int)W});
           } else if (fmt == FMT_PIPE) {
-            const int warps = pipe_warps_for(P, sms);
+            const int warps = pipe_warps_for(P, sms, vsz);
             const int gth = 32 * (warps - 2);
             const size_t fixed = al16(8 * 8) + al16(vsz * (3 * BS + 2 * (size_t)gth));
             // the ring the pieces are cut for, the smallest one (4) where a
@@ -1789,8 +1964,7 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       a.nbuf = kW2Ring;
       a.bufbytes = (int)bufbytes;
       a.wmask = (uint32_t)D.stage_window[st] - 1u;
-      a.per_warp = (int)al16(al16(8 * (size_t)kW2Ring) + BS * sizeof(VT) + (size_t)kW2Ring * bufbytes +
-                             (size_t)D.stage_window[st] * sizeof(VT));
+      a.per_warp = (int)w2_warp_bytes<VT>(kW2Ring, bufbytes, (size_t)D.stage_window[st]);
       a.pf = prefetch_distance(P.knobs.w2_pf);
       if (a.pf) a.pf = std::max(a.pf, kW2Ring);  // the offset cache holds records k+NB .. k+NB+63
       if ((size_t)a.per_warp > kSmemCap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
