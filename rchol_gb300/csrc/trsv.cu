@@ -1424,7 +1424,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
             for (int u = 0; u < kPipePre; ++u) {
               const bool ok = (uint32_t)u < s_n1;
               pc[u] = ok ? (uint32_t)s_n1c[u * BS + lane] : 0u;
-              pv[u] = ok ? -s_n1v[u * BS + lane] : VT(0);
+              pv[u] = ok ? s_n1v[u * BS + lane] : VT(0);
             }
           }
           pos.next(RING);
