@@ -710,59 +710,52 @@ void build_w2_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &
 
 // ---- pipeline format: one thread block per piece --------------------------------------
 //
-// For the few long chains at the top of the tree.  Block k's entries in
-// earlier blocks of the piece are split by distance so that each step of the
-// chain carries as little as possible:
-//   distance 1 (block k-1) the solver warp, with the inverse: x_k = T^-1 t,
-//                          t = u_k - N1 x_{k-1};
-//   distance 2 (block k-2) the reducer warp, one step ahead:
-//                          u_k = acc_k - sum of chunk sums - N2 x_{k-2};
-//   distance >= 3          the gatherer warps, two steps ahead: chunk sums
-//                          over columns solved before block k-2.
+// For the few long chains at the top of the tree.  With t = acc - (entries in
+// earlier blocks)·x and N1 / N2 / F the block's entries in the previous block,
+// the one before and older ones,
+//   x_k = T^-1 t = w_k + y_k - P_k x_{k-1},
+//   w_k = T^-1 (acc_k - F_k x),  y_k = -Q_k x_{k-2},  P = T^-1 N1,  Q = T^-1 N2,
+// with P and Q computed in FP64 on the host.  Each term is prepared by its
+// own warp as soon as its inputs exist, so the chain of the solver warp in
+// step k is one shared-memory read (w + y) and 32 FMAs with P's row and
+// x_{k-1}, both already in its registers.
 // Record (16-byte sections):
-//   u32 hdr[16]   nrows, row0, prow0, pprow0, n1, n2, nchunk, clen, col_bytes,
-//                 o_n1c, o_n1v, o_n2c, o_n2v, o_crow, o_fc, o_fv
-//   VT  tinv[576]                       packed inverse (at byte 64)
-//   u8  n1c[n1][32];  VT n1v[n1][32]    slot-major: entry j of row r at j*32 + r,
-//   u8  n2c[n2][32];  VT n2v[n2][32]    column within block k-1 / k-2 (padding 0, 0)
-//   u16 crow[33]                        row r's chunks [crow[r], crow[r+1])
-//   u16|u32 fc[clen][nchunk]; VT fv[..] entry j of chunk c at j*nchunk + c
+//   u32 hdr[16]  nrows, row0, prow0, pprow0, nchunk, clen, col_bytes, o_crow,
+//                o_fc, o_fv, stride (P / Q row stride in values), 0...
+//   VT  tinv[576]                 packed inverse (at byte 64), the reducer's
+//   VT  P[32][stride], Q[32][stride]  dense, rows padded (conflict-free
+//                                 16-byte row reads by 32 lanes)
+//   u16 crow[33]                  row r's chunks [crow[r], crow[r+1])
+//   u16|u32 fc[clen][nchunk]; VT fv[..]  far entries, entry j of chunk c at j*nchunk + c
+__host__ __device__ inline int pq_stride(size_t vsz) { return vsz == 4 ? 36 : 34; }
+constexpr int kPipeRoleWarps = 3;  // solver, reducer, mixer; the other warps of a team gather
+
 struct PipeLayout {
-  size_t o_n1c, o_n1v, o_n2c, o_n2v, o_crow, o_fc, o_fv, len;
+  size_t o_tinv, o_p, o_q, o_crow, o_fc, o_fv, len;
 };
 
-__host__ __device__ inline PipeLayout pipe_layout(uint32_t n1, uint32_t n2, uint32_t nchunk, uint32_t clen,
-                                                  uint32_t csz, uint32_t vsz) {
+__host__ __device__ inline PipeLayout pipe_layout(uint32_t nchunk, uint32_t clen, uint32_t csz, uint32_t vsz) {
   PipeLayout L;
-  size_t o = 64 + (size_t)vsz * 4 * TQ;
-  L.o_n1c = o;
-  o += al16((size_t)BS * n1);
-  L.o_n1v = o;
-  o += al16((size_t)vsz * BS * n1);
-  L.o_n2c = o;
-  o += al16((size_t)BS * n2);
-  L.o_n2v = o;
-  o += al16((size_t)vsz * BS * n2);
-  L.o_crow = o;
-  o += al16(2 * (BS + 1));
-  L.o_fc = o;
-  o += al16((size_t)csz * nchunk * clen);
-  L.o_fv = o;
-  o += al16((size_t)vsz * nchunk * clen);
-  L.len = o;
+  const size_t pq = (size_t)vsz * BS * pq_stride(vsz);
+  L.o_tinv = 64;
+  L.o_p = L.o_tinv + (size_t)vsz * 4 * TQ;
+  L.o_q = L.o_p + pq;
+  L.o_crow = L.o_q + pq;
+  L.o_fc = L.o_crow + al16(2 * (BS + 1));
+  L.o_fv = L.o_fc + al16((size_t)csz * nchunk * clen);
+  L.len = L.o_fv + al16((size_t)vsz * nchunk * clen);
   return L;
 }
 
-// Upper bound of a pipeline record whose block's rows have at most n1 / n2
-// entries in the previous block / the one before and `far` entries in older
-// blocks of its piece, for `gthreads` gatherer threads (cutting the node into
-// pieces only moves entries out of a record).
-inline size_t pipe_record_bound(uint32_t n1, uint32_t n2, size_t far, size_t gthreads, size_t vsz, size_t csz) {
+// Upper bound of a pipeline record whose block has `far` entries more than
+// two blocks back in its piece, for `gthreads` gatherer threads (cutting the
+// node into pieces only moves entries out of a record).
+inline size_t pipe_record_bound(size_t far, size_t gthreads, size_t vsz, size_t csz) {
   const size_t slots = gthreads > (size_t)BS ? gthreads - BS : 1;
   const size_t clen = std::max<size_t>(1, (far + slots - 1) / slots);
   const size_t padded = far + BS * clen;
-  return 64 + vsz * 4 * TQ + al16((size_t)BS * n1) + al16(vsz * BS * n1) + al16((size_t)BS * n2) +
-         al16(vsz * BS * n2) + al16(2 * (BS + 1)) + al16(csz * padded) + al16(vsz * padded);
+  return 64 + vsz * 4 * TQ + 2 * vsz * BS * pq_stride(vsz) + al16(2 * (BS + 1)) + al16(csz * padded) +
+         al16(vsz * padded);
 }
 
 void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, const std::vector<double> &v,
@@ -770,11 +763,12 @@ void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
                       int32_t &maxchunk) {
   const int64_t R = e - b, nb = (R + BS - 1) / BS;
   const uint32_t csz = R > 65535 ? 4 : 2;
+  const int stride = pq_stride(vsz);
   P.offs.assign(1, 0);
   P.bytes.clear();
   maxchunk = 0;
-  double T[BS][BS], X[BS][BS];
-  std::vector<std::pair<uint32_t, double>> l1[BS], l2[BS], lf[BS];
+  double T[BS][BS], X[BS][BS], N1[BS][BS], N2[BS][BS];
+  std::vector<std::pair<uint32_t, double>> lf[BS];
   for (int64_t s = 0; s < nb; ++s) {
     const int64_t bi = upper ? nb - 1 - s : s;
     const int64_t row0 = bi * BS;
@@ -782,13 +776,11 @@ void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
     const int64_t b1 = upper ? bi + 1 : bi - 1, b2 = upper ? bi + 2 : bi - 2;  // blocks k-1, k-2
     const bool has1 = s >= 1, has2 = s >= 2;
     for (int r = 0; r < BS; ++r) {
-      for (int c = 0; c < BS; ++c) T[r][c] = 0.0;
+      for (int c = 0; c < BS; ++c) T[r][c] = N1[r][c] = N2[r][c] = 0.0;
       T[r][r] = 1.0;
-      l1[r].clear();
-      l2[r].clear();
       lf[r].clear();
     }
-    uint32_t nfar = 0, n1 = 0, n2 = 0;
+    uint32_t nfar = 0;
     for (int r = 0; r < nr; ++r) {
       const int64_t i = b + row0 + r;
       for (int64_t q = rp[i]; q < rp[i + 1]; ++q) {
@@ -796,15 +788,13 @@ void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
         if (c < b || c >= e) continue;  // external
         const int64_t lc = c - b, cb = lc / BS;
         if (cb == bi) T[r][lc - row0] = v[q];
-        else if (has1 && cb == b1) l1[r].push_back({(uint32_t)(lc - b1 * BS), v[q]});
-        else if (has2 && cb == b2) l2[r].push_back({(uint32_t)(lc - b2 * BS), v[q]});
+        else if (has1 && cb == b1) N1[r][lc - b1 * BS] = v[q];
+        else if (has2 && cb == b2) N2[r][lc - b2 * BS] = v[q];
         else {
           lf[r].push_back({(uint32_t)lc, v[q]});
           ++nfar;
         }
       }
-      n1 = std::max<uint32_t>(n1, (uint32_t)l1[r].size());
-      n2 = std::max<uint32_t>(n2, (uint32_t)l2[r].size());
     }
     invert_block(T, upper, X);
     // far entries in chunks of clen (a row's last chunk padded), one chunk
@@ -820,27 +810,31 @@ void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
     }
     if (nchunk > (uint32_t)gthreads) throw Error(RCHOL_ERR_INTERNAL, "pipeline record: more chunks than gatherers");
     maxchunk = std::max<int32_t>(maxchunk, (int32_t)nchunk);
-    const PipeLayout L = pipe_layout(n1, n2, nchunk, clen, csz, (uint32_t)vsz);
+    const PipeLayout L = pipe_layout(nchunk, clen, csz, (uint32_t)vsz);
     const size_t base = P.bytes.size();
     P.bytes.resize(base + L.len, 0);
     unsigned char *p = P.bytes.data() + base;
     const int64_t prow0 = has1 ? b1 * BS : 0, pprow0 = has2 ? b2 * BS : 0;
-    const uint32_t hdr[16] = {(uint32_t)nr,       (uint32_t)row0,     (uint32_t)prow0,    (uint32_t)pprow0,
-                              n1,                 n2,                 nchunk,             clen,
-                              csz,                (uint32_t)L.o_n1c,  (uint32_t)L.o_n1v,  (uint32_t)L.o_n2c,
-                              (uint32_t)L.o_n2v,  (uint32_t)L.o_crow, (uint32_t)L.o_fc,   (uint32_t)L.o_fv};
+    const uint32_t hdr[16] = {(uint32_t)nr,      (uint32_t)row0,    (uint32_t)prow0,  (uint32_t)pprow0,
+                              nchunk,            clen,              csz,              (uint32_t)L.o_crow,
+                              (uint32_t)L.o_fc,  (uint32_t)L.o_fv,  (uint32_t)stride, 0,
+                              0,                 0,                 0,                0};
     std::memcpy(p, hdr, sizeof(hdr));
-    put_tinv(p + 64, vsz, X, nr, upper);
-    for (int r = 0; r < BS; ++r) {
-      for (size_t j = 0; j < l1[r].size(); ++j) {
-        p[L.o_n1c + j * BS + r] = (unsigned char)l1[r][j].first;
-        put_val(p + L.o_n1v, vsz, j * BS + r, l1[r][j].second);
+    put_tinv(p + L.o_tinv, vsz, X, nr, upper);
+    // P = T^-1 N1, Q = T^-1 N2 (rows and columns beyond the block's rows are zero)
+    for (int r = 0; r < BS; ++r)
+      for (int c = 0; c < BS; ++c) {
+        double pr = 0.0, qr = 0.0;
+        if (r < nr)
+          for (int k = 0; k < nr; ++k) {
+            const double t = X[r][k];
+            if (t == 0.0) continue;
+            pr += t * N1[k][c];
+            qr += t * N2[k][c];
+          }
+        put_val(p + L.o_p, vsz, (size_t)r * stride + c, pr);
+        put_val(p + L.o_q, vsz, (size_t)r * stride + c, qr);
       }
-      for (size_t j = 0; j < l2[r].size(); ++j) {
-        p[L.o_n2c + j * BS + r] = (unsigned char)l2[r][j].first;
-        put_val(p + L.o_n2v, vsz, j * BS + r, l2[r][j].second);
-      }
-    }
     std::memcpy(p + L.o_crow, crow, sizeof(crow));
     // chunk c holds row r's far entries crow[r]*clen.. in column order; within
     // each warp's 32 chunks the entries of one step are picked greedily so that
@@ -902,7 +896,8 @@ void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
     P.offs.push_back((int64_t)P.bytes.size());
     P.maxrec = std::max<int32_t>(P.maxrec, (int32_t)L.len);
     P.sparse += nfar;
-    for (int r = 0; r < BS; ++r) P.sparse += l1[r].size() + l2[r].size();
+    for (int r = 0; r < BS; ++r)
+      for (int c = 0; c < BS; ++c) P.sparse += (N1[r][c] != 0.0) + (N2[r][c] != 0.0);
   }
 }
 
@@ -1155,6 +1150,10 @@ struct RingPos {
   }
 };
 
+// Block-wide barrier 0 over `n` threads, usable from the different loops of
+// warp-specialised code (each thread of the block arrives once per use).
+__device__ __forceinline__ void cta_barrier(unsigned n) { asm volatile("bar.sync 0, %0;\n" ::"r"(n) : "memory"); }
+
 template <int SZ>
 __device__ __forceinline__ void cp_async_small(void *smem, const void *gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -1289,7 +1288,7 @@ struct PipeArgs {
   const NodeDesc *nodes;
   int node0;         // piece = node0 + blockIdx.x
   int bufbytes;      // bytes of a ring slot (16-aligned)
-  int ring;          // ring slots (4..8): records k, k+1, k+2 in use, the rest in flight
+  int ring;          // ring slots (4..8): records k+1, k+2 in use, the rest in flight
   int maxchunk;      // most chunks of one block (chunk-sum buffer)
   int pf;            // records prefetched into L2 ahead of use
   const unsigned char *blocks;
@@ -1297,41 +1296,49 @@ struct PipeArgs {
   const VT *acc;     // rhs minus external sums, or null: the stage reads `in`
 };
 
-// distance-1 entries per row the solver loads before the step's barrier
-// (fewer for FP64, whose inverse row already takes 64 registers)
-template <typename VT>
-__host__ __device__ constexpr int pipe_pre() {
-  return sizeof(VT) == 4 ? 8 : 4;
-}
-
-// One thread block per piece: warp 0 solves, warp 1 reduces, warps 2..
-// gather, warp 2 also streams the records.  One __syncthreads per step; in
-// step s the solver retires block s, the reducer prepares u for block s+1,
-// the gatherers sum the far entries of block s+2.  Everything of block s+1
-// that does not depend on block s -- its header, inverse row and first
-// distance-1 entries -- the solver loads before the barrier.  The piece's
-// right-hand side and then its solution live in shared memory (xs).
-// FP64 teams have at most 12 warps (170 registers a thread: the inverse row
-// alone takes 64)
+// FP64 teams have at most 12 warps (170 registers a thread)
 template <typename VT>
 __host__ __device__ constexpr int pipe_max_threads() {
   return sizeof(VT) == 8 ? 384 : 512;
 }
 
+// Shared memory of pipe_kernel besides the record ring: the mbarriers, then
+// the reducer's broadcast buffer t[32], w[2][32], y[2][32], the chunk sums
+// [2][maxchunk], and after the ring the piece's vector padded to whole blocks.
+template <typename VT>
+__host__ __device__ inline size_t pipe_vec_bytes(int maxchunk) {
+  return al16(sizeof(VT) * (5 * BS + 2 * (size_t)maxchunk));
+}
+
+// One thread block per piece.  In step s:
+//   warp 0 (solver)   x_s = w_s + y_s - P_s x_{s-1}, with P_s's row and the
+//                     broadcast x_{s-1} in registers; then reads x_s back as
+//                     eight broadcast quads and P_{s+1}'s row;
+//   warp 1 (reducer)  w_{s+1} = T^-1 (acc - chunk sums) of block s+1, then
+//                     the inverse row of block s+2;
+//   warp 2 (mixer)    y_{s+1} = -Q_{s+1} x_{s-1}; streams record s+RING into
+//                     the slot of record s and, one thread, waits for record
+//                     s+3 (the barrier then publishes it to every warp);
+//   warps 3..         far chunk sums of block s+2.
+// One __syncthreads per step.  The piece's right-hand side, then its
+// solution, live in shared memory (xs).
 template <typename VT, typename InT, typename OutT, bool UPPER>
 __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArgs<VT> a, const InT *__restrict__ in,
-                                                      OutT *__restrict__ out) {
+                                                                         OutT *__restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int abort_flag;
   const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int RING = a.ring, nb = nd.nblocks;
+  const int stride = pq_stride(sizeof(VT));
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-  VT *tsh = reinterpret_cast<VT *>(smem + al16(8 * (size_t)RING));
-  VT *ubuf = tsh + BS;                    // [2][32]
-  VT *part = ubuf + 2 * BS;               // [2][maxchunk]
-  unsigned char *ring = reinterpret_cast<unsigned char *>(tsh) + al16(sizeof(VT) * (3 * BS + 2 * (size_t)a.maxchunk));
+  VT *tb = reinterpret_cast<VT *>(smem + al16(8 * (size_t)RING));
+  VT *wbuf = tb + BS;        // [2][32]
+  VT *ybuf = wbuf + 2 * BS;  // [2][32]
+  VT *part = ybuf + 2 * BS;  // [2][maxchunk]
+  unsigned char *ring = reinterpret_cast<unsigned char *>(tb) + pipe_vec_bytes<VT>(a.maxchunk);
   VT *xs = reinterpret_cast<VT *>(ring + (size_t)RING * a.bufbytes);
+  const int rows_pad = (nd.rows + BS - 1) / BS * BS;
   OffCache oc;
   if (warp == 2) oc.init(a.blk_off + nd.blk0, nb, lane);
   if (tid == 0) {
@@ -1339,8 +1346,9 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     for (int i = 0; i < RING; ++i) mbar_init(bar + i, 1);
     fence_mbar_init();
   }
-  // the piece's right-hand side into shared memory, eight loads in flight per thread
-  for (int r0 = tid; r0 < nd.rows; r0 += 8 * (int)blockDim.x) {
+  // the piece's right-hand side into shared memory (zeros past its rows),
+  // eight loads in flight per thread
+  for (int r0 = tid; r0 < rows_pad; r0 += 8 * (int)blockDim.x) {
     VT v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -1350,145 +1358,171 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int r = r0 + u * (int)blockDim.x;
-      if (r < nd.rows) xs[r] = v[u];
+      if (r < rows_pad) xs[r] = v[u];
     }
   }
   __syncthreads();
   auto slot_ptr = [&](int slot) { return ring + (size_t)slot * a.bufbytes; };
-  RingPos ld;  // warp 2: slot of the next record to issue
-  uint32_t issued = 0;
-  auto issue = [&](int k) {  // warp 2: record k into the next slot
+  // warp 2: records go into every slot first, then record k into the slot of
+  // record k - RING; lane 0 waits for record k three steps before use
+  RingPos ld, wt;
+  int issued = 0, waited = 0;
+  auto issue = [&](int k) {
     const int64_t o0 = oc.get(k), o1 = oc.get(k + 1);
     if (lane == 0) bulk_load(slot_ptr(ld.slot), a.blocks + o0, (uint32_t)(o1 - o0), bar + ld.slot);
     ld.next(RING);
-    issued = (uint32_t)(k + 1);
+    issued = k + 1;
   };
-  if (warp == 2)
-    for (int k = 0; k < RING - 3 && k < nb; ++k) issue(k);
-  auto wait_at = [&](const RingPos &q) {
-    if (!mbar_wait(bar + q.slot, q.par)) {
+  auto wait_next = [&]() {  // warp 2 lane 0: the next record in order
+    if (!mbar_wait(bar + wt.slot, wt.par)) {
       atomicOr(&g_solve_status, 1u);
       abort_flag = 1;
-      return false;
     }
-    return true;
+    wt.next(RING);
+    ++waited;
   };
-  RingPos pos;  // the next record this thread's role reads
-  // solver: block s+1 loaded ahead of the barrier
-  VT m[BS];
-  constexpr int kPipePre = pipe_pre<VT>();
-  uint32_t s_nr = 0, s_row0 = 0, s_prow0 = 0, s_n1 = 0, pc[kPipePre];
-  VT pv[kPipePre];
-  const unsigned char *s_n1c = nullptr;
-  const VT *s_n1v = nullptr;
-  for (int s = -2; s < nb; ++s) {
-    const bool stop = abort_flag != 0;  // read after the last barrier: uniform
-    if (!stop) {
-      if (warp == 0) {
+  if (warp == 2) {
+    for (int k = 0; k < RING && k < nb; ++k) issue(k);
+    if (lane == 0)
+      while (waited < 3 && waited < nb && !abort_flag) wait_next();
+  }
+  __syncthreads();
+  // Each role runs its own loop over the steps (registers are then allocated
+  // per role); every loop passes the same block-wide barrier once per step,
+  // after which abort_flag is read: uniform across the block.
+  const unsigned nthreads = blockDim.x;
+  if (warp == 0) {  // solver: P row of its next block and the broadcast x of its last one
+    VT pr[BS], xb[BS];
+#pragma unroll
+    for (int c = 0; c < BS; ++c) xb[c] = VT(0);
+    uint32_t s_nr = 0, s_row0 = 0;
+    for (int s = -2; s < nb; ++s) {
+      if (!abort_flag) {
         if (s >= 0) {
-          VT g[kPipePre];
+          VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
-          for (int u = 0; u < kPipePre; ++u) g[u] = xs[s_prow0 + pc[u]];
-          VT a0 = 0, a1 = 0;
-#pragma unroll
-          for (int u = 0; u < kPipePre; u += 2) {
-            a0 = fma(pv[u], g[u], a0);
-            a1 = fma(pv[u + 1], g[u + 1], a1);
+          for (int c = 0; c < BS; c += 4) {
+            a0 = fma(pr[c], xb[c], a0);
+            a1 = fma(pr[c + 1], xb[c + 1], a1);
+            a2 = fma(pr[c + 2], xb[c + 2], a2);
+            a3 = fma(pr[c + 3], xb[c + 3], a3);
           }
-          VT near = a0 + a1;
-          if (s_n1 > (uint32_t)kPipePre)
-            near += slot_dot(s_n1c + kPipePre * BS, s_n1v + kPipePre * BS, xs, s_prow0, s_n1 - kPipePre, lane);
-          const VT u = lane < (int)s_nr ? ubuf[(s & 1) * BS + lane] : VT(0);
-          tsh[lane] = lane < (int)s_nr ? u - near : VT(0);
-          __syncwarp();
-          const VT x = apply_row(m, tsh);
+          const VT x = (wbuf[(s & 1) * BS + lane] + ybuf[(s & 1) * BS + lane]) - ((a0 + a1) + (a2 + a3));
           if (lane < (int)s_nr) {
             xs[s_row0 + lane] = x;
             out[nd.begin + s_row0 + lane] = (OutT)x;
           }
-        }
-        if (s + 1 >= 0 && s + 1 < nb) {  // block s+1: everything that does not depend on block s
-          if (wait_at(pos)) {
-            const unsigned char *p = slot_ptr(pos.slot);
-            const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
-            const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
-            const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
-            s_nr = h0.x;
-            s_row0 = h0.y;
-            s_prow0 = h0.z;
-            s_n1 = h1.x;
-            s_n1c = p + h2.y;
-            s_n1v = reinterpret_cast<const VT *>(p + h2.z);
-            load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + 64), lane, m);
+          __syncwarp();
 #pragma unroll
-            for (int u = 0; u < kPipePre; ++u) {
-              const bool ok = (uint32_t)u < s_n1;
-              pc[u] = ok ? (uint32_t)s_n1c[u * BS + lane] : 0u;
-              pv[u] = ok ? s_n1v[u * BS + lane] : VT(0);
-            }
+          for (int q = 0; q < 8; ++q) {
+            VT t[4];
+            ld_quad(xs + s_row0 + 4 * q, t);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xb[4 * q + u] = t[u];
           }
-          pos.next(RING);
         }
-      } else if (warp == 1) {
-        const int bk = s + 1;  // reducer: u of block s+1
+        if (s + 1 >= 0 && s + 1 < nb) {  // block s+1: header and P's row
+          const unsigned char *p = slot_ptr((s + 1) % RING);
+          const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
+          s_nr = h0.x;
+          s_row0 = h0.y;
+          const VT *P = reinterpret_cast<const VT *>(p + 64 + sizeof(VT) * 4 * TQ) + lane * stride;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            VT t[4];
+            ld_quad(P + 4 * q, t);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) pr[4 * q + u] = t[u];
+          }
+        }
+      }
+      cta_barrier(nthreads);
+    }
+  } else if (warp == 1) {  // reducer: w of block s+1
+    for (int s = -2; s < nb; ++s) {
+      const int bk = s + 1;
+      if (!abort_flag && bk >= 0 && bk < nb) {
+        const unsigned char *p = slot_ptr(bk % RING);
+        VT m[BS];
+        load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + 64), lane, m);
+        const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
+        const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
+        const uint32_t nr = h0.x, row0 = h0.y;
+        const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h1.w);
+        const VT far = range_sum(part + (size_t)(bk & 1) * a.maxchunk, crow[lane], crow[lane + 1]);
+        tb[lane] = lane < (int)nr ? xs[row0 + lane] - far : VT(0);
+        __syncwarp();
+        wbuf[(bk & 1) * BS + lane] = apply_row(m, tb);
+      }
+      cta_barrier(nthreads);
+    }
+  } else if (warp == 2) {  // mixer: y of block s+1 = -Q x of block s-1; streams the records
+    for (int s = -2; s < nb; ++s) {
+      if (!abort_flag) {
+        const int bk = s + 1;
         if (bk >= 0 && bk < nb) {
-          if (wait_at(pos)) {
-            const unsigned char *p = slot_ptr(pos.slot);
-            const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
-            const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
-            const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
-            const uint4 h3 = *reinterpret_cast<const uint4 *>(p + 48);
-            const uint32_t nr = h0.x, row0 = h0.y, pprow0 = h0.w, n2 = h1.y;
-            const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h3.y);
-            const VT *pb = part + (size_t)(bk & 1) * a.maxchunk;
-            const VT acc0 = lane < (int)nr ? xs[row0 + lane] : VT(0);
-            const VT far = range_sum(pb, crow[lane], crow[lane + 1]);
-            const VT mid = slot_dot(p + h2.w, reinterpret_cast<const VT *>(p + h3.x), xs, pprow0, n2, lane);
-            ubuf[(bk & 1) * BS + lane] = lane < (int)nr ? acc0 - (far + mid) : VT(0);
+          VT y = VT(0);
+          if (bk >= 2) {
+            const unsigned char *p = slot_ptr(bk % RING);
+            const uint32_t pprow0 = reinterpret_cast<const uint32_t *>(p)[3];
+            const VT *Q = reinterpret_cast<const VT *>(p + 64 + sizeof(VT) * (4 * TQ + (size_t)BS * stride)) +
+                          lane * stride;
+            VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              VT qq[4], xx[4];
+              ld_quad(Q + 4 * q, qq);
+              ld_quad(xs + pprow0 + 4 * q, xx);
+              a0 = fma(qq[0], xx[0], a0);
+              a1 = fma(qq[1], xx[1], a1);
+              a2 = fma(qq[2], xx[2], a2);
+              a3 = fma(qq[3], xx[3], a3);
+            }
+            y = -((a0 + a1) + (a2 + a3));
           }
-          pos.next(RING);
+          ybuf[(bk & 1) * BS + lane] = y;
         }
-      } else {
-        if (warp == 2) {  // stream record s-1+RING into the slot of record s-1 (retired last step)
-          const int k = s - 1 + RING;
+        if (s >= 0) {  // record s+RING into the slot of record s (free since the last barrier)
+          const int k = s + RING;
           oc.advance(a.pf ? min(k, s + a.pf) : k, lane);  // the lowest record index used this step
-          if (k >= RING - 3 && k < nb) {
+          if (k < nb) {
             if (lane == 0) fence_proxy_async();
             issue(k);
           }
-          if (a.pf && s + a.pf >= 0 && s + a.pf < nb) {
+          if (a.pf && s + a.pf < nb) {
             const int64_t o0 = oc.get(s + a.pf), o1 = oc.get(s + a.pf + 1);
             if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
           }
-        }
-        const int bk = s + 2;  // gatherers: far sums of block s+2
-        if (bk < nb) {
-          if (wait_at(pos)) {
-            const unsigned char *p = slot_ptr(pos.slot);
-            const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
-            const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
-            const uint4 h3 = *reinterpret_cast<const uint4 *>(p + 48);
-            const uint32_t nchunk = h1.z, clen = h1.w, csz = h2.x;
-            const int g = tid - 64;
-            if (g < (int)nchunk) {
-              const VT *fv = reinterpret_cast<const VT *>(p + h3.w);
-              part[(size_t)(bk & 1) * a.maxchunk + g] =
-                  csz == 2 ? chunk_dot(reinterpret_cast<const uint16_t *>(p + h3.z), fv, xs, (uint32_t)g, nchunk, clen)
-                           : chunk_dot(reinterpret_cast<const uint32_t *>(p + h3.z), fv, xs, (uint32_t)g, nchunk, clen);
-            }
-          }
-          pos.next(RING);
+          if (lane == 0 && s + 3 < nb) wait_next();  // record s+3, read from the next step on
         }
       }
+      cta_barrier(nthreads);
     }
-    __syncthreads();
+  } else {  // gatherers: far sums of block s+2
+    const int g = tid - 32 * kPipeRoleWarps;
+    for (int s = -2; s < nb; ++s) {
+      const int bk = s + 2;
+      if (!abort_flag && bk < nb) {
+        const unsigned char *p = slot_ptr(bk % RING);
+        const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
+        const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
+        const uint32_t nchunk = h1.x, clen = h1.y, csz = h1.z;
+        if (g < (int)nchunk) {
+          const VT *fv = reinterpret_cast<const VT *>(p + h2.y);
+          part[(size_t)(bk & 1) * a.maxchunk + g] =
+              csz == 2 ? chunk_dot(reinterpret_cast<const uint16_t *>(p + h2.x), fv, xs, (uint32_t)g, nchunk, clen)
+                       : chunk_dot(reinterpret_cast<const uint32_t *>(p + h2.x), fv, xs, (uint32_t)g, nchunk, clen);
+        }
+      }
+      cta_barrier(nthreads);
+    }
   }
   if (abort_flag && warp == 2 && lane == 0) {
-    // copies that may still be in flight: the last RING issued, one per slot
-    RingPos q;
-    for (int j = 0; j < (int)issued; ++j) {
-      if (j >= (int)issued - RING) (void)mbar_wait(bar + q.slot, q.par);
-      q.next(RING);
+    // copies that may still be in flight: those issued and not waited for (one per slot)
+    while (waited < issued) {
+      (void)mbar_wait(bar + wt.slot, wt.par);
+      wt.next(RING);
+      ++waited;
     }
   }
 }
@@ -1580,7 +1614,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
       n2 = std::max(n2, m2);
     }
     if (fmt == FMT_WARP) return w2_record_bound(cnt, vsz, csz);
-    if (fmt == FMT_PIPE) return pipe_record_bound(n1, n2, far, (size_t)gth, vsz, csz);
+    if (fmt == FMT_PIPE) return pipe_record_bound(far, (size_t)gth, vsz, csz);
     return team_record_bound(cnt, (size_t)gth, vsz, csz);
   };
   // Cuts a node into pieces of whole blocks whose shared memory fits:
@@ -1654,8 +1688,8 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
             for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_WARP, 1, (int)W});
           } else if (fmt == FMT_PIPE) {
             const int warps = pipe_warps_for(P, sms, vsz);
-            const int gth = 32 * (warps - 2);
-            const size_t fixed = al16(8 * 8) + al16(vsz * (3 * BS + 2 * (size_t)gth));
+            const int gth = 32 * (warps - kPipeRoleWarps);
+            const size_t fixed = al16(8 * 8) + al16(vsz * (5 * BS + 2 * (size_t)gth)) + BS * vsz;  // + block padding
             // the ring the pieces are cut for, the smallest one (4) where a
             // single block's record would not fit a deeper one
             ok = cut(v, fmt, gth, fixed, kPipeRingCut, vsz, 1 << 30, kSmemCap, rng);
@@ -1736,7 +1770,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
         if (reach + BS >= pc.window && pc.window < pc.e - pc.b)
           throw Error(RCHOL_ERR_INTERNAL, "warp-format window shorter than the piece's reach");
       } else if (pc.fmt == FMT_PIPE) {
-        build_pipe_piece(rp, ci, v, pc.b, pc.e, upper, vsz, 32 * (pc.warps - 2), built[k], chunks[k]);
+        build_pipe_piece(rp, ci, v, pc.b, pc.e, upper, vsz, 32 * (pc.warps - kPipeRoleWarps), built[k], chunks[k]);
       } else {
         build_team_piece(rp, ci, v, pc.b, pc.e, upper, vsz, 32 * (pc.warps - 1), true, built[k], chunks[k]);
       }
@@ -1987,7 +2021,7 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       a.maxchunk = D.stage_chunks[st];
       a.pf = prefetch_distance(pieces <= sms ? P.knobs.pipe_pf : 0);
       const int warps = D.stage_warps[st];
-      const size_t fixed0 = al16(sizeof(VT) * (3 * BS + 2 * (size_t)a.maxchunk)) + (size_t)D.stage_rows[st] * sizeof(VT);
+      const size_t fixed0 = pipe_vec_bytes<VT>(a.maxchunk) + (size_t)(D.stage_rows[st] + BS - 1) / BS * BS * sizeof(VT);
       int ring = std::max(4, std::min(8, P.knobs.pipe_ring));
       while (ring > 4 && al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes > kSmemCap) --ring;
       a.ring = ring;

@@ -5,10 +5,10 @@
 // then executes them on the CPU in the order the kernels do: per stage the
 // external entries, then per piece block after block.  Warp format: every
 // column a row reads must be solved and still held by the window of solved
-// values.  Pipeline format: the kernel's three-step schedule -- in step s the
-// gatherers sum block s+2's far entries from columns solved before step s,
-// the reducer prepares block s+1 with its entries in block s-1, the solver
-// retires block s with its entries in block s-1.  32-wide (k-team) format:
+// values.  Pipeline format: the kernel's schedule -- in step s the gatherers
+// sum block s+2's far entries from columns solved before step s, the reducer
+// forms w = T^-1 (acc - far) of block s+1, the mixer y = -Q x of block s+1
+// from block s-1, the solver retires block s as w + y - P x of block s-1.  32-wide (k-team) format:
 // helpers one block ahead, the solver with the previous block.  A record that
 // reads a column not solved at that point would race on the GPU and fails
 // the check; the results are compared with plain substitution on the CSR of G.
@@ -182,35 +182,49 @@ std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &
       } else if (fmt == FMT_PIPE) {
         ++team_pieces;
         // the kernel's schedule: in step s the gatherers sum block s+2's far
-        // entries, the reducer prepares u of block s+1, the solver retires block s
-        std::vector<std::vector<VT>> part(2);
-        std::vector<VT> u(2 * BS, (VT)NAN);
+        // entries, the reducer forms w = T^-1 (acc - far) of block s+1, the
+        // mixer y = -Q x of block s+1 from block s-1, the solver retires block
+        // s as w + y - P x of block s-1
         const int nb = nd.nblocks;
+        std::vector<std::vector<VT>> part(2);
+        std::vector<VT> wv(2 * BS, (VT)NAN), yv(2 * BS, (VT)NAN);
         auto hdr_of = [&](int b, uint32_t h[16]) {
           const unsigned char *p = rec(b);
           std::memcpy(h, p, 64);
-          const PipeLayout L = pipe_layout(h[4], h[5], h[6], h[7], h[8], vsz);
+          const PipeLayout L = pipe_layout(h[4], h[5], h[6], vsz);
           if ((int64_t)L.len != rec_len(b)) fail("pipeline record length", (long)L.len, b);
           if ((int)L.len > nd.maxrec) fail("record above the piece's maximum", (long)L.len, nd.maxrec);
-          if (h[9] != L.o_n1c || h[10] != L.o_n1v || h[11] != L.o_n2c || h[12] != L.o_n2v || h[13] != L.o_crow ||
-              h[14] != L.o_fc || h[15] != L.o_fv)
+          if (h[7] != L.o_crow || h[8] != L.o_fc || h[9] != L.o_fv || h[10] != (uint32_t)pq_stride(vsz))
             fail("pipeline record offsets", b, 0);
-          if ((int)h[6] > nd.maxchunk) fail("chunks above the piece's maximum", h[6], nd.maxchunk);
+          if ((int)h[4] > nd.maxchunk) fail("chunks above the piece's maximum", h[4], nd.maxchunk);
           return p;
+        };
+        // dense 32x32 matrix (row stride `stride`) times the 32 unknowns of a
+        // block solved in step `when`; every nonzero column must be such an unknown
+        auto dense_mul = [&](const unsigned char *M, int r, uint32_t base, int when, int b, const char *what) {
+          const int stride = pq_stride(vsz);
+          VT acc = 0;
+          for (int c = 0; c < BS; ++c) {
+            const VT m = ld<VT>(M, (size_t)r * stride + c);
+            if (m == (VT)0) continue;
+            if (base + c >= (uint32_t)nd.rows || solved_at[base + c] != when) fail(what, c, b);
+            acc += m * xs[base + c];
+          }
+          return acc;
         };
         for (int s = -2; s < nb; ++s) {
           std::vector<VT> newpart;
           if (s + 2 < nb) {  // gatherers
             uint32_t h[16];
             const unsigned char *p = hdr_of(s + 2, h);
-            const uint32_t nchunk = h[6], clen = h[7], csz = h[8];
+            const uint32_t nchunk = h[4], clen = h[5], csz = h[6];
             newpart.assign(nchunk, 0);
             for (uint32_t c = 0; c < nchunk; ++c) {
               VT s0 = 0, s1 = 0;
               for (uint32_t j = 0; j < clen; ++j) {
                 const size_t at = (size_t)j * nchunk + c;
-                const uint32_t col = col_at(p + h[14], at, csz);
-                const VT val = ld<VT>(p + h[15], at);
+                const uint32_t col = col_at(p + h[8], at, csz);
+                const VT val = ld<VT>(p + h[9], at);
                 if (col >= (uint32_t)nd.rows) fail("far column outside the piece", col, s + 2);
                 if (val != (VT)0 && (solved_at[col] < 0 || solved_at[col] > s - 1))
                   fail("far column not solved before the step", col, s + 2);
@@ -219,58 +233,53 @@ std::vector<double> emulate(const HostStreamCopy &H, const std::vector<double> &
               newpart[c] = s0 + s1;
             }
           }
-          std::vector<VT> newu;
-          if (s + 1 >= 0 && s + 1 < nb) {  // reducer
+          std::vector<VT> neww, newy;
+          if (s + 1 >= 0 && s + 1 < nb) {  // reducer and mixer
             const int bk = s + 1;
             uint32_t h[16];
             const unsigned char *p = hdr_of(bk, h);
-            const uint32_t nr = h[0], row0 = h[1], pprow0 = h[3], n2 = h[5];
+            const uint32_t nr = h[0], row0 = h[1], pprow0 = h[3];
             uint16_t crow[BS + 1];
-            std::memcpy(crow, p + h[13], sizeof(crow));
-            if (crow[BS] != h[6]) fail("chunk rows", crow[BS], h[6]);
+            std::memcpy(crow, p + h[7], sizeof(crow));
+            if (crow[BS] != h[4]) fail("chunk rows", crow[BS], h[4]);
             const std::vector<VT> &pb = part[bk & 1];
-            if (pb.size() != h[6]) fail("chunk sums not prepared", bk, (long)pb.size());
-            newu.assign(BS, 0);
+            if (pb.size() != h[4]) fail("chunk sums not prepared", bk, (long)pb.size());
+            VT t[BS] = {};
             for (uint32_t r = 0; r < nr; ++r) {
-              VT u0 = xs[row0 + r], u1 = 0;
               if (solved_at[row0 + r] >= 0) fail("reducer row already solved", row0 + r, bk);
-              for (uint32_t c = crow[r]; c < crow[r + 1]; ++c) ((c - crow[r]) & 1 ? u1 : u0) -= pb[c];
-              for (uint32_t j = 0; j < n2; ++j) {
-                const uint32_t c = p[h[11] + (size_t)j * BS + r];
-                const VT val = ld<VT>(p + h[12], (size_t)j * BS + r);
-                if (c >= (uint32_t)BS) fail("distance-2 column", c, bk);
-                if (val != (VT)0 && (bk < 2 || pprow0 + c >= (uint32_t)nd.rows || solved_at[pprow0 + c] != bk - 2))
-                  fail("distance-2 column not in block k-2", c, bk);
-                (j & 1 ? u1 : u0) -= val * xs[pprow0 + c];
-              }
-              newu[r] = u0 + u1;
+              VT f0 = 0, f1 = 0;
+              for (uint32_t c = crow[r]; c < crow[r + 1]; ++c) ((c - crow[r]) & 1 ? f1 : f0) -= pb[c];
+              t[r] = xs[row0 + r] + (f0 + f1);
             }
+            neww.assign(BS, 0);
+            apply_tinv<VT>(p + 64, t, neww.data(), upper);
+            newy.assign(BS, 0);
+            const PipeLayout L = pipe_layout(h[4], h[5], h[6], vsz);
+            for (int r = 0; r < BS; ++r)
+              newy[r] = bk >= 2 ? -dense_mul(p + L.o_q, r, pprow0, s - 1, bk, "distance-2 column not in block k-2")
+                                : (VT)0;
           }
           if (s >= 0) {  // solver
             uint32_t h[16];
             const unsigned char *p = hdr_of(s, h);
-            const uint32_t nr = h[0], row0 = h[1], prow0 = h[2], n1 = h[4];
-            VT t[BS] = {}, x[BS];
-            for (uint32_t r = 0; r < nr; ++r) {
-              VT t0 = u[(s & 1) * BS + r], t1 = 0;
-              if (std::isnan((double)t0)) fail("u not prepared", r, s);
-              for (uint32_t j = 0; j < n1; ++j) {
-                const uint32_t c = p[h[9] + (size_t)j * BS + r];
-                const VT val = ld<VT>(p + h[10], (size_t)j * BS + r);
-                if (c >= (uint32_t)BS) fail("distance-1 column", c, s);
-                if (val != (VT)0 && (s < 1 || prow0 + c >= (uint32_t)nd.rows || solved_at[prow0 + c] != s - 1))
-                  fail("distance-1 column not in block k-1", c, s);
-                (j & 1 ? t1 : t0) -= val * xs[prow0 + c];
-              }
-              t[r] = t0 + t1;
+            const uint32_t nr = h[0], row0 = h[1], prow0 = h[2];
+            const PipeLayout L = pipe_layout(h[4], h[5], h[6], vsz);
+            VT x[BS];
+            for (int r = 0; r < BS; ++r) {
+              if (std::isnan((double)wv[(s & 1) * BS + r]) || std::isnan((double)yv[(s & 1) * BS + r]))
+                fail("w or y not prepared", r, s);
+              const VT px = s >= 1 ? dense_mul(p + L.o_p, r, prow0, s - 1, s, "distance-1 column not in block k-1")
+                                   : (VT)0;
+              x[r] = (wv[(s & 1) * BS + r] + yv[(s & 1) * BS + r]) - px;
             }
-            apply_tinv<VT>(p + 64, t, x, upper);
             finish(s, nr, row0, x);
           }
           if (s + 2 < nb) part[(s + 2) & 1] = newpart;
-          if (s + 1 >= 0 && s + 1 < nb) {
-            for (int r = 0; r < BS; ++r) u[((s + 1) & 1) * BS + r] = newu[r];
-          }
+          if (s + 1 >= 0 && s + 1 < nb)
+            for (int r = 0; r < BS; ++r) {
+              wv[((s + 1) & 1) * BS + r] = neww[r];
+              yv[((s + 1) & 1) * BS + r] = newy[r];
+            }
         }
       } else {
         ++team_pieces;
