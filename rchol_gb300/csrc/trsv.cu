@@ -728,7 +728,7 @@ void build_w2_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &
 //   u16 crow[33]                  row r's chunks [crow[r], crow[r+1])
 //   u16|u32 fc[clen][nchunk]; VT fv[..]  far entries, entry j of chunk c at j*nchunk + c
 __host__ __device__ inline int pq_stride(size_t vsz) { return vsz == 4 ? 36 : 34; }
-constexpr int kPipeRoleWarps = 3;  // solver, reducer, mixer; the other warps of a team gather
+constexpr int kPipeRoleWarps = 3;  // solver, reducer, mixer; the other warps of a team gather (at least one)
 
 struct PipeLayout {
   size_t o_tinv, o_p, o_q, o_crow, o_fc, o_fv, len;
@@ -1288,7 +1288,7 @@ struct PipeArgs {
   const NodeDesc *nodes;
   int node0;         // piece = node0 + blockIdx.x
   int bufbytes;      // bytes of a ring slot (16-aligned)
-  int ring;          // ring slots (4..8): records k+1, k+2 in use, the rest in flight
+  int ring;          // ring slots (5..8): records k+1..k+3 in use, k+4 waited for, the rest in flight
   int maxchunk;      // most chunks of one block (chunk-sum buffer)
   int pf;            // records prefetched into L2 ahead of use
   const unsigned char *blocks;
@@ -1340,7 +1340,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
   VT *xs = reinterpret_cast<VT *>(ring + (size_t)RING * a.bufbytes);
   const int rows_pad = (nd.rows + BS - 1) / BS * BS;
   OffCache oc;
-  if (warp == 2) oc.init(a.blk_off + nd.blk0, nb, lane);
+  if (warp == 3) oc.init(a.blk_off + nd.blk0, nb, lane);
   if (tid == 0) {
     abort_flag = 0;
     for (int i = 0; i < RING; ++i) mbar_init(bar + i, 1);
@@ -1363,8 +1363,11 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
   }
   __syncthreads();
   auto slot_ptr = [&](int slot) { return ring + (size_t)slot * a.bufbytes; };
-  // warp 2: records go into every slot first, then record k into the slot of
-  // record k - RING; lane 0 waits for record k three steps before use
+  // warp 3 (the first gatherer warp) streams the records: into every slot
+  // first, then record k into the slot of record k - RING; its lane 0 waits
+  // for record k four steps before use, so that after the next barrier every
+  // warp may read records up to k (each role loads its next step's operands
+  // a step ahead).
   RingPos ld, wt;
   int issued = 0, waited = 0;
   auto issue = [&](int k) {
@@ -1373,7 +1376,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     ld.next(RING);
     issued = k + 1;
   };
-  auto wait_next = [&]() {  // warp 2 lane 0: the next record in order
+  auto wait_next = [&]() {  // warp 3 lane 0: the next record in order
     if (!mbar_wait(bar + wt.slot, wt.par)) {
       atomicOr(&g_solve_status, 1u);
       abort_flag = 1;
@@ -1381,21 +1384,22 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     wt.next(RING);
     ++waited;
   };
-  if (warp == 2) {
+  if (warp == 3) {
     for (int k = 0; k < RING && k < nb; ++k) issue(k);
     if (lane == 0)
-      while (waited < 3 && waited < nb && !abort_flag) wait_next();
+      while (waited < 4 && waited < nb && !abort_flag) wait_next();
   }
   __syncthreads();
   // Each role runs its own loop over the steps (registers are then allocated
   // per role); every loop passes the same block-wide barrier once per step,
   // after which abort_flag is read: uniform across the block.
   const unsigned nthreads = blockDim.x;
-  if (warp == 0) {  // solver: P row of its next block and the broadcast x of its last one
+  if (warp == 0) {  // solver: x_s = w_s + y_s - P_s x_{s-1}
     VT pr[BS], xb[BS];
 #pragma unroll
     for (int c = 0; c < BS; ++c) xb[c] = VT(0);
     uint32_t s_nr = 0, s_row0 = 0;
+    RingPos rp;  // record of the solver's next block
     for (int s = -2; s < nb; ++s) {
       if (!abort_flag) {
         if (s >= 0) {
@@ -1422,7 +1426,8 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
           }
         }
         if (s + 1 >= 0 && s + 1 < nb) {  // block s+1: header and P's row
-          const unsigned char *p = slot_ptr((s + 1) % RING);
+          const unsigned char *p = slot_ptr(rp.slot);
+          rp.next(RING);
           const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
           s_nr = h0.x;
           s_row0 = h0.y;
@@ -1438,51 +1443,129 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
       }
       cta_barrier(nthreads);
     }
-  } else if (warp == 1) {  // reducer: w of block s+1
+  } else if (warp == 1) {  // reducer: w of block s+1 = T^-1 (acc - chunk sums)
+    VT m[BS];                // inverse row of block s+1, loaded in step s-1
+    uint32_t r_nr = 0, r_row0 = 0, c0 = 0, c1 = 0;
+    RingPos rp;
+    auto load_next = [&](VT (&mm)[BS], uint32_t &nr, uint32_t &row0, uint32_t &a0, uint32_t &a1) {
+      const unsigned char *p = slot_ptr(rp.slot);
+      rp.next(RING);
+      load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + 64), lane, mm);
+      const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
+      const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
+      const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h1.w);
+      nr = h0.x;
+      row0 = h0.y;
+      a0 = crow[lane];
+      a1 = crow[lane + 1];
+    };
+    if (nb > 0) load_next(m, r_nr, r_row0, c0, c1);  // block 0 (records 0..3 are in)
     for (int s = -2; s < nb; ++s) {
       const int bk = s + 1;
       if (!abort_flag && bk >= 0 && bk < nb) {
-        const unsigned char *p = slot_ptr(bk % RING);
-        VT m[BS];
-        load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + 64), lane, m);
-        const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
-        const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
-        const uint32_t nr = h0.x, row0 = h0.y;
-        const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h1.w);
-        const VT far = range_sum(part + (size_t)(bk & 1) * a.maxchunk, crow[lane], crow[lane + 1]);
-        tb[lane] = lane < (int)nr ? xs[row0 + lane] - far : VT(0);
+        // the next block's operands first (independent of this step's data)
+        VT mn[BS];
+        uint32_t nr2 = 0, row02 = 0, c02 = 0, c12 = 0;
+        const bool more = bk + 1 < nb;
+        if (more) load_next(mn, nr2, row02, c02, c12);
+        const VT far = range_sum(part + (size_t)(bk & 1) * a.maxchunk, c0, c1);
+        tb[lane] = lane < (int)r_nr ? xs[r_row0 + lane] - far : VT(0);
         __syncwarp();
         wbuf[(bk & 1) * BS + lane] = apply_row(m, tb);
+        if (more) {
+#pragma unroll
+          for (int c = 0; c < BS; ++c) m[c] = mn[c];
+          r_nr = nr2;
+          r_row0 = row02;
+          c0 = c02;
+          c1 = c12;
+        }
       }
       cta_barrier(nthreads);
     }
-  } else if (warp == 2) {  // mixer: y of block s+1 = -Q x of block s-1; streams the records
+  } else if (warp == 2) {  // mixer: y of block s+1 = -Q x of block s-1
+    VT qr[BS];               // Q's row of block s+1, loaded in step s-1
+    uint32_t m_pprow0 = 0;
+    RingPos rp;
+    auto load_next = [&](VT (&qq)[BS], uint32_t &pprow0) {
+      const unsigned char *p = slot_ptr(rp.slot);
+      rp.next(RING);
+      pprow0 = reinterpret_cast<const uint32_t *>(p)[3];
+      const VT *Q = reinterpret_cast<const VT *>(p + 64 + sizeof(VT) * (4 * TQ + (size_t)BS * stride)) + lane * stride;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        VT t[4];
+        ld_quad(Q + 4 * q, t);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) qq[4 * q + u] = t[u];
+      }
+    };
+    if (nb > 0) load_next(qr, m_pprow0);
+    for (int s = -2; s < nb; ++s) {
+      const int bk = s + 1;
+      if (!abort_flag && bk >= 0 && bk < nb) {
+        VT qn[BS];
+        uint32_t pp2 = 0;
+        const bool more = bk + 1 < nb;
+        if (more) load_next(qn, pp2);
+        VT y = VT(0);
+        if (bk >= 2) {
+          VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            VT xx[4];
+            ld_quad(xs + m_pprow0 + 4 * q, xx);
+            a0 = fma(qr[4 * q + 0], xx[0], a0);
+            a1 = fma(qr[4 * q + 1], xx[1], a1);
+            a2 = fma(qr[4 * q + 2], xx[2], a2);
+            a3 = fma(qr[4 * q + 3], xx[3], a3);
+          }
+          y = -((a0 + a1) + (a2 + a3));
+        }
+        ybuf[(bk & 1) * BS + lane] = y;
+        if (more) {
+#pragma unroll
+          for (int c = 0; c < BS; ++c) qr[c] = qn[c];
+          m_pprow0 = pp2;
+        }
+      }
+      cta_barrier(nthreads);
+    }
+  } else {  // gatherers: far sums of block s+2; warp 3 also streams the records
+    const int g = tid - 32 * kPipeRoleWarps;
+    RingPos rp;
+    rp.next(RING);
+    rp.next(RING);  // record 2: the gatherers' first block in step 0 (blocks 0, 1 have no far entries)
+    // chunk g of the next block: its first kPipeGPre entries' columns and values
+    constexpr int GP = 4;
+    uint32_t gcol[GP] = {0, 0, 0, 0}, nchunk = 0, clen = 0, csz = 2, o_fc = 0, o_fv = 0;
+    VT gval[GP] = {VT(0), VT(0), VT(0), VT(0)};
+    const unsigned char *gp = nullptr;
+    auto load_next = [&](int bk) {  // block bk's header and this thread's first entries
+      gp = slot_ptr(rp.slot);
+      rp.next(RING);
+      const uint4 h1 = *reinterpret_cast<const uint4 *>(gp + 16);
+      const uint4 h2 = *reinterpret_cast<const uint4 *>(gp + 32);
+      nchunk = h1.x;
+      clen = h1.y;
+      csz = h1.z;
+      o_fc = h2.x;
+      o_fv = h2.y;
+      (void)bk;
+#pragma unroll
+      for (int u = 0; u < GP; ++u) {
+        const bool ok = g < (int)nchunk && (uint32_t)u < clen;
+        const uint32_t at = (uint32_t)u * nchunk + (uint32_t)g;
+        gcol[u] = !ok ? 0u
+                      : csz == 2 ? (uint32_t)reinterpret_cast<const uint16_t *>(gp + o_fc)[at]
+                                 : reinterpret_cast<const uint32_t *>(gp + o_fc)[at];
+        gval[u] = ok ? reinterpret_cast<const VT *>(gp + o_fv)[at] : VT(0);
+      }
+    };
+    if (nb > 2) load_next(2);
     for (int s = -2; s < nb; ++s) {
       if (!abort_flag) {
-        const int bk = s + 1;
-        if (bk >= 0 && bk < nb) {
-          VT y = VT(0);
-          if (bk >= 2) {
-            const unsigned char *p = slot_ptr(bk % RING);
-            const uint32_t pprow0 = reinterpret_cast<const uint32_t *>(p)[3];
-            const VT *Q = reinterpret_cast<const VT *>(p + 64 + sizeof(VT) * (4 * TQ + (size_t)BS * stride)) +
-                          lane * stride;
-            VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              VT qq[4], xx[4];
-              ld_quad(Q + 4 * q, qq);
-              ld_quad(xs + pprow0 + 4 * q, xx);
-              a0 = fma(qq[0], xx[0], a0);
-              a1 = fma(qq[1], xx[1], a1);
-              a2 = fma(qq[2], xx[2], a2);
-              a3 = fma(qq[3], xx[3], a3);
-            }
-            y = -((a0 + a1) + (a2 + a3));
-          }
-          ybuf[(bk & 1) * BS + lane] = y;
-        }
-        if (s >= 0) {  // record s+RING into the slot of record s (free since the last barrier)
+        if (warp == 3 && s >= 0) {  // record s+RING into the slot of record s (free since the last barrier)
           const int k = s + RING;
           oc.advance(a.pf ? min(k, s + a.pf) : k, lane);  // the lowest record index used this step
           if (k < nb) {
@@ -1493,31 +1576,40 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
             const int64_t o0 = oc.get(s + a.pf), o1 = oc.get(s + a.pf + 1);
             if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
           }
-          if (lane == 0 && s + 3 < nb) wait_next();  // record s+3, read from the next step on
+          if (lane == 0 && s + 4 < nb) wait_next();  // record s+4, read from the next step on
         }
-      }
-      cta_barrier(nthreads);
-    }
-  } else {  // gatherers: far sums of block s+2
-    const int g = tid - 32 * kPipeRoleWarps;
-    for (int s = -2; s < nb; ++s) {
-      const int bk = s + 2;
-      if (!abort_flag && bk < nb) {
-        const unsigned char *p = slot_ptr(bk % RING);
-        const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
-        const uint4 h2 = *reinterpret_cast<const uint4 *>(p + 32);
-        const uint32_t nchunk = h1.x, clen = h1.y, csz = h1.z;
-        if (g < (int)nchunk) {
-          const VT *fv = reinterpret_cast<const VT *>(p + h2.y);
-          part[(size_t)(bk & 1) * a.maxchunk + g] =
-              csz == 2 ? chunk_dot(reinterpret_cast<const uint16_t *>(p + h2.x), fv, xs, (uint32_t)g, nchunk, clen)
-                       : chunk_dot(reinterpret_cast<const uint32_t *>(p + h2.x), fv, xs, (uint32_t)g, nchunk, clen);
+        const int bk = s + 2;
+        if (bk >= 2 && bk < nb) {
+          // this step: the preloaded entries of block bk, the rest from the record
+          if (g < (int)nchunk) {
+            VT xg[GP];
+#pragma unroll
+            for (int u = 0; u < GP; ++u) xg[u] = xs[gcol[u]];
+            VT a0 = 0, a1 = 0;
+#pragma unroll
+            for (int u = 0; u < GP; u += 2) {
+              a0 = fma(gval[u], xg[u], a0);
+              a1 = fma(gval[u + 1], xg[u + 1], a1);
+            }
+            VT sum = a0 + a1;
+            if (clen > (uint32_t)GP) {
+              const uint32_t base = (uint32_t)GP * nchunk + (uint32_t)g;
+              const VT *fv = reinterpret_cast<const VT *>(gp + o_fv) + (uint32_t)GP * nchunk;
+              sum += csz == 2 ? chunk_dot(reinterpret_cast<const uint16_t *>(gp + o_fc) + (uint32_t)GP * nchunk, fv, xs,
+                                          (uint32_t)g, nchunk, clen - GP)
+                              : chunk_dot(reinterpret_cast<const uint32_t *>(gp + o_fc) + (uint32_t)GP * nchunk, fv, xs,
+                                          (uint32_t)g, nchunk, clen - GP);
+              (void)base;
+            }
+            part[(size_t)(bk & 1) * a.maxchunk + g] = sum;
+          }
+          if (bk + 1 < nb) load_next(bk + 1);
         }
       }
       cta_barrier(nthreads);
     }
   }
-  if (abort_flag && warp == 2 && lane == 0) {
+  if (abort_flag && warp == 3 && lane == 0) {
     // copies that may still be in flight: those issued and not waited for (one per slot)
     while (waited < issued) {
       (void)mbar_wait(bar + wt.slot, wt.par);
@@ -1560,6 +1652,7 @@ constexpr int kW2Ring = 4;                   // warp format: record slots per wa
 constexpr int kW2WindowMax = 8192;           // warp format: most rows in a window
 constexpr size_t kW2WarpBudget = 56 * 1024;  // warp format: shared memory of one warp (at least 4 warps per SM)
 constexpr int kPipeRingCut = 6;              // pipeline format: ring the pieces are cut for (launch: up to 8)
+constexpr int kPipeRingMin = 5;              // pipeline format: records k+1..k+3 in use, k+4 waited for, one in flight
 
 // Pipeline team size of a stage with `pieces` pieces: 16 warps where at
 // most one piece runs per SM, fewer (several teams per SM) beyond.
@@ -1690,12 +1783,12 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
             const int warps = pipe_warps_for(P, sms, vsz);
             const int gth = 32 * (warps - kPipeRoleWarps);
             const size_t fixed = al16(8 * 8) + al16(vsz * (5 * BS + 2 * (size_t)gth)) + BS * vsz;  // + block padding
-            // the ring the pieces are cut for, the smallest one (4) where a
+            // the ring the pieces are cut for, the smallest one where a
             // single block's record would not fit a deeper one
             ok = cut(v, fmt, gth, fixed, kPipeRingCut, vsz, 1 << 30, kSmemCap, rng);
             if (!ok) {
               rng.clear();
-              ok = cut(v, fmt, gth, fixed, 4, vsz, 1 << 30, kSmemCap, rng);
+              ok = cut(v, fmt, gth, fixed, kPipeRingMin, vsz, 1 << 30, kSmemCap, rng);
             }
             for (auto &r : rng) per_node[j].push_back(Piece{r.first, r.second, FMT_PIPE, warps, 0});
           } else {
@@ -2022,8 +2115,8 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       a.pf = prefetch_distance(pieces <= sms ? P.knobs.pipe_pf : 0);
       const int warps = D.stage_warps[st];
       const size_t fixed0 = pipe_vec_bytes<VT>(a.maxchunk) + (size_t)(D.stage_rows[st] + BS - 1) / BS * BS * sizeof(VT);
-      int ring = std::max(4, std::min(8, P.knobs.pipe_ring));
-      while (ring > 4 && al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes > kSmemCap) --ring;
+      int ring = std::max(kPipeRingMin, std::min(8, P.knobs.pipe_ring));
+      while (ring > kPipeRingMin && al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes > kSmemCap) --ring;
       a.ring = ring;
       const size_t bytes = al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes;
       if (bytes > kSmemCap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
@@ -2093,7 +2186,7 @@ std::pair<double, double> tune_solves(const rchol_factor_s &F, SolvePlan &P, cud
     P.knobs.*field = pick;
   };
   try_knob(&SolveKnobs::pipe_pf, {0, 8, 16, 24});
-  try_knob(&SolveKnobs::pipe_ring, {4, 6, 8});
+  try_knob(&SolveKnobs::pipe_ring, {5, 6, 8});
   try_knob(&SolveKnobs::w2_wpb, {1, 2, 4, 8});
   try_knob(&SolveKnobs::w2_pf, {0, 8, 16});
   cudaEventDestroy(e0);
