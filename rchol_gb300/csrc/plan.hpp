@@ -110,7 +110,7 @@ struct SegWork {
 struct SolveKnobs {
   int pipe_pf = 24;   // pipeline format: records prefetched into L2 ahead of use (0: none)
   int w2_pf = 0;      // warp format: the same
-  int pipe_ring = 8;  // pipeline format: most ring slots (4..8)
+  int pipe_ring = 8;  // pipeline format: most ring slots (5..8)
   int w2_wpb = 8;     // warp format: most warps (pieces) per thread block (1..8)
 };
 

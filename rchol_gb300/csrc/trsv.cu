@@ -1232,35 +1232,89 @@ __global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__rest
     cp_async_commit();
   };
   for (int k = 0; k < kW2RhsRing - 1; ++k) fetch_rhs(k);
-  RingPos pos;
-  int k = 0;
-  bool ok = true;
-  for (; k < nb; ++k) {
-    fetch_rhs(k + kW2RhsRing - 1);
-    ok = __all_sync(0xffffffffu, mbar_wait(bar + pos.slot, pos.par));
-    if (!ok) break;
-    cp_async_wait<kW2RhsRing - 1>();  // block k's right-hand side (this lane's own copy) is in
-    const unsigned char *p = ring + (size_t)pos.slot * a.bufbytes;
+  // Block k+1's operands (header, inverse row, row offsets and the lane's
+  // first kW2Pre entries) are loaded while block k is solved; the chain of a
+  // step is then the gathers from the window and the broadcast of t.
+  constexpr int kW2Pre = sizeof(VT) == 4 ? 8 : 4;
+  struct Ops {
+    uint32_t nr, row0, e0, e1, csz, o_tinv;
+    const unsigned char *p;
+    const VT *val;
+    uint32_t c[kW2Pre];
+    VT v[kW2Pre];
+  };
+  auto load_ops = [&](int slot, Ops &o) {
+    const unsigned char *p = ring + (size_t)slot * a.bufbytes;
     const uint4 h = *reinterpret_cast<const uint4 *>(p);
-    const uint32_t nr = h.x, row0 = h.y, nent = h.z, csz = h.w;
-    const W2Layout L = w2_layout(nent, csz, sizeof(VT));
-    VT m[BS];
-    load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + L.o_tinv), lane, m);
+    o.p = p;
+    o.nr = h.x;
+    o.row0 = h.y;
+    o.csz = h.w;
+    const W2Layout L = w2_layout(h.z, h.w, sizeof(VT));
     const uint16_t *eoff = reinterpret_cast<const uint16_t *>(p + L.o_eoff);
-    const VT *val = reinterpret_cast<const VT *>(p + L.o_val);
-    const uint32_t e0 = eoff[lane], e1 = eoff[lane + 1];
-    const VT sum = csz == 2 ? run_dot(reinterpret_cast<const uint16_t *>(p + L.o_col), val, xw, wmask, e0, e1)
-                            : run_dot(reinterpret_cast<const uint32_t *>(p + L.o_col), val, xw, wmask, e0, e1);
+    o.e0 = eoff[lane];
+    o.e1 = eoff[lane + 1];
+    o.val = reinterpret_cast<const VT *>(p + L.o_val);
+    o.o_tinv = (uint32_t)L.o_tinv;
+#pragma unroll
+    for (int u = 0; u < kW2Pre; ++u) {
+      const uint32_t e = o.e0 + u;
+      const bool ok = e < o.e1;
+      o.c[u] = !ok ? 0u
+                   : o.csz == 2 ? (uint32_t)reinterpret_cast<const uint16_t *>(p + L.o_col)[e]
+                                : reinterpret_cast<const uint32_t *>(p + L.o_col)[e];
+      o.v[u] = ok ? o.val[e] : VT(0);
+    }
+  };
+  RingPos pos;  // slot of block k
+  int k = 0;
+  bool ok = __all_sync(0xffffffffu, nb == 0 || mbar_wait(bar + 0, 0u));
+  Ops cur;
+  if (ok && nb > 0) load_ops(0, cur);
+  for (; ok && k < nb; ++k) {
+    fetch_rhs(k + kW2RhsRing - 1);
+    // the window's values for block k's preloaded entries first (the chain)
+    VT g[kW2Pre];
+#pragma unroll
+    for (int u = 0; u < kW2Pre; ++u) g[u] = xw[cur.c[u] & wmask];
+    VT m[BS];  // block k's inverse row, after the gathers in the load queue
+    load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(cur.p + cur.o_tinv), lane, m);
+    RingPos nxt = pos;
+    nxt.next(NB);
+    Ops nx;
+    const bool more = k + 1 < nb;
+    if (more) {
+      ok = __all_sync(0xffffffffu, mbar_wait(bar + nxt.slot, nxt.par));
+      if (!ok) break;
+      load_ops(nxt.slot, nx);
+    }
+    VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+    for (int u = 0; u < kW2Pre; u += 4) {
+      a0 = fma(cur.v[u], g[u], a0);
+      a1 = fma(cur.v[u + 1], g[u + 1], a1);
+      a2 = fma(cur.v[u + 2], g[u + 2], a2);
+      a3 = fma(cur.v[u + 3], g[u + 3], a3);
+    }
+    VT sum = (a0 + a1) + (a2 + a3);
+    if (cur.e1 > cur.e0 + kW2Pre) {  // the rest of a long row
+      const W2Layout L = w2_layout(0, cur.csz, sizeof(VT));
+      sum += cur.csz == 2
+                 ? run_dot(reinterpret_cast<const uint16_t *>(cur.p + L.o_col), cur.val, xw, wmask, cur.e0 + kW2Pre, cur.e1)
+                 : run_dot(reinterpret_cast<const uint32_t *>(cur.p + L.o_col), cur.val, xw, wmask, cur.e0 + kW2Pre,
+                           cur.e1);
+    }
+    cp_async_wait<kW2RhsRing - 1>();  // block k's right-hand side (this lane's own copy) is in
     const void *rp = rq + (k & (kW2RhsRing - 1)) * BS + lane;
     const VT q0 = a.acc ? *reinterpret_cast<const VT *>(rp) : (VT) * reinterpret_cast<const InT *>(rp);
-    tsh[lane] = lane < (int)nr ? q0 - sum : VT(0);
+    tsh[lane] = lane < (int)cur.nr ? q0 - sum : VT(0);
     __syncwarp();
     const VT x = apply_row(m, tsh);
-    if (lane < (int)nr) {
-      xw[(row0 + lane) & wmask] = x;
-      out[nd.begin + row0 + lane] = (OutT)x;
+    if (lane < (int)cur.nr) {
+      xw[(cur.row0 + lane) & wmask] = x;
+      out[nd.begin + cur.row0 + lane] = (OutT)x;
     }
-    __syncwarp();  // slot and tsh free again
+    __syncwarp();  // block k's slot and tsh free again
     oc.advance(k + NB, lane);  // the lowest record index used below
     if (k + NB < nb) {
       if (lane == 0) fence_proxy_async();
@@ -1270,7 +1324,8 @@ __global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__rest
       const int64_t o0 = oc.get(k + a.pf), o1 = oc.get(k + a.pf + 1);
       if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
     }
-    pos.next(NB);
+    pos = nxt;
+    if (more) cur = nx;
   }
   if (!ok) {  // give up: wait (bounded) for the copies still in flight, one per slot
     if (lane == 0) {
@@ -1463,23 +1518,13 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     for (int s = -2; s < nb; ++s) {
       const int bk = s + 1;
       if (!abort_flag && bk >= 0 && bk < nb) {
-        // the next block's operands first (independent of this step's data)
-        VT mn[BS];
-        uint32_t nr2 = 0, row02 = 0, c02 = 0, c12 = 0;
-        const bool more = bk + 1 < nb;
-        if (more) load_next(mn, nr2, row02, c02, c12);
+        // this step's reads first: shared-memory requests are served in
+        // order, so the next block's operands are loaded after them
         const VT far = range_sum(part + (size_t)(bk & 1) * a.maxchunk, c0, c1);
         tb[lane] = lane < (int)r_nr ? xs[r_row0 + lane] - far : VT(0);
         __syncwarp();
         wbuf[(bk & 1) * BS + lane] = apply_row(m, tb);
-        if (more) {
-#pragma unroll
-          for (int c = 0; c < BS; ++c) m[c] = mn[c];
-          r_nr = nr2;
-          r_row0 = row02;
-          c0 = c02;
-          c1 = c12;
-        }
+        if (bk + 1 < nb) load_next(m, r_nr, r_row0, c0, c1);
       }
       cta_barrier(nthreads);
     }
@@ -1504,10 +1549,6 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     for (int s = -2; s < nb; ++s) {
       const int bk = s + 1;
       if (!abort_flag && bk >= 0 && bk < nb) {
-        VT qn[BS];
-        uint32_t pp2 = 0;
-        const bool more = bk + 1 < nb;
-        if (more) load_next(qn, pp2);
         VT y = VT(0);
         if (bk >= 2) {
           VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
@@ -1523,11 +1564,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
           y = -((a0 + a1) + (a2 + a3));
         }
         ybuf[(bk & 1) * BS + lane] = y;
-        if (more) {
-#pragma unroll
-          for (int c = 0; c < BS; ++c) qr[c] = qn[c];
-          m_pprow0 = pp2;
-        }
+        if (bk + 1 < nb) load_next(qr, m_pprow0);  // after this step's reads (served in order)
       }
       cta_barrier(nthreads);
     }
