@@ -1209,6 +1209,9 @@ __global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__rest
     for (int i = 0; i < NB; ++i) mbar_init(bar + i, 1);
     fence_mbar_init();
   }
+  // padding entries (value 0) read the window at column 0: it starts at zero
+  // so that they add 0, never 0 times stale shared memory
+  for (uint32_t i = lane; i <= wmask; i += 32) xw[i] = VT(0);
   __syncwarp();
   auto issue = [&](int k, int slot) {  // all lanes (offset shuffles); lane 0 copies record k
     const int64_t o0 = oc.get(k), o1 = oc.get(k + 1);
