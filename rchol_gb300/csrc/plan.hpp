@@ -108,7 +108,7 @@ struct SegWork {
 // setting solves the same system with the same arithmetic; the tuner
 // (rchol_gpu_factor_tune) times alternatives on the factor itself.
 struct SolveKnobs {
-  int pipe_pf = 24;   // pipeline format: records prefetched into L2 ahead of use (0: none)
+  int pipe_pf = 0;    // pipeline format: records prefetched into L2 ahead of use (0: none)
   int w2_pf = 0;      // warp format: the same
   int pipe_ring = 8;  // pipeline format: most ring slots (5..8)
   int w2_wpb = 8;     // warp format: most warps (pieces) per thread block (1..8)

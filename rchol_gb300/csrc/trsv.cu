@@ -727,8 +727,11 @@ void build_w2_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &
 //                                 16-byte row reads by 32 lanes)
 //   u16 crow[33]                  row r's chunks [crow[r], crow[r+1])
 //   u16|u32 fc[clen][nchunk]; VT fv[..]  far entries, entry j of chunk c at j*nchunk + c
-__host__ __device__ inline int pq_stride(size_t vsz) { return vsz == 4 ? 36 : 34; }
-constexpr int kPipeRoleWarps = 3;  // solver, reducer, mixer; the other warps of a team gather (at least one)
+__host__ __device__ constexpr int pq_stride(size_t vsz) { return vsz == 4 ? 36 : 34; }
+// byte offset of crow: fixed by the value size
+__host__ __device__ constexpr size_t pipe_o_crow(size_t vsz) { return 64 + vsz * 4 * TQ + 2 * vsz * BS * pq_stride(vsz); }
+constexpr int kPipeRoleWarps = 4;  // solver, reducer, mixer, record streamer; the other warps of a team gather
+constexpr int kPipeRowChunks = 8;  // most chunks of one row's far entries
 
 struct PipeLayout {
   size_t o_tinv, o_p, o_q, o_crow, o_fc, o_fv, len;
@@ -740,22 +743,38 @@ __host__ __device__ inline PipeLayout pipe_layout(uint32_t nchunk, uint32_t clen
   L.o_tinv = 64;
   L.o_p = L.o_tinv + (size_t)vsz * 4 * TQ;
   L.o_q = L.o_p + pq;
-  L.o_crow = L.o_q + pq;
+  L.o_crow = L.o_q + pq;  // == pipe_o_crow(vsz)
   L.o_fc = L.o_crow + al16(2 * (BS + 1));
   L.o_fv = L.o_fc + al16((size_t)csz * nchunk * clen);
   L.len = L.o_fv + al16((size_t)vsz * nchunk * clen);
   return L;
 }
 
-// Upper bound of a pipeline record whose block has `far` entries more than
-// two blocks back in its piece, for `gthreads` gatherer threads (cutting the
-// node into pieces only moves entries out of a record).
-inline size_t pipe_record_bound(size_t far, size_t gthreads, size_t vsz, size_t csz) {
-  const size_t slots = gthreads > (size_t)BS ? gthreads - BS : 1;
-  const size_t clen = std::max<size_t>(1, (far + slots - 1) / slots);
-  const size_t padded = far + BS * clen;
-  return 64 + vsz * 4 * TQ + 2 * vsz * BS * pq_stride(vsz) + al16(2 * (BS + 1)) + al16(csz * padded) +
-         al16(vsz * padded);
+// Chunking of a pipeline record's far entries (`rf[r]` of row r, `nfar` in
+// all): chunks of clen entries (a row's last chunk padded), one chunk per
+// gatherer thread (every row adds at most one partial chunk, so
+// ceil(nfar / (gthreads - 32)) entries per chunk suffice), and no row in more
+// than kPipeRowChunks chunks, so that the reducer's lane for a row sums its
+// chunks in one batch of loads.
+struct PipeChunks {
+  uint32_t clen, nchunk;
+};
+inline PipeChunks pipe_chunks(const uint32_t *rf, uint32_t nfar, int gthreads) {
+  const uint32_t slots = (uint32_t)std::max(1, gthreads - BS);
+  uint32_t longest = 0;
+  for (int r = 0; r < BS; ++r) longest = std::max(longest, rf[r]);
+  PipeChunks c;
+  c.clen = std::max<uint32_t>({1u, (nfar + slots - 1) / slots, (longest + kPipeRowChunks - 1) / kPipeRowChunks});
+  c.nchunk = 0;
+  for (int r = 0; r < BS; ++r) c.nchunk += (rf[r] + c.clen - 1) / c.clen;
+  return c;
+}
+
+// Length of a pipeline record whose rows have `rf[r]` entries more than two
+// blocks back in their piece, for `gthreads` gatherer threads.
+inline size_t pipe_record_len(const uint32_t *rf, uint32_t nfar, int gthreads, size_t vsz, size_t csz) {
+  const PipeChunks c = pipe_chunks(rf, nfar, gthreads);
+  return pipe_layout(c.nchunk, c.clen, (uint32_t)csz, (uint32_t)vsz).len;
 }
 
 void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci, const std::vector<double> &v,
@@ -797,20 +816,17 @@ void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
       }
     }
     invert_block(T, upper, X);
-    // far entries in chunks of clen (a row's last chunk padded), one chunk
-    // per gatherer thread: every row adds at most one partial chunk
-    const int slots = std::max(1, gthreads - BS);
-    const uint32_t clen = std::max<uint32_t>(1, (nfar + slots - 1) / slots);
+    uint32_t rf[BS];
+    for (int r = 0; r < BS; ++r) rf[r] = (uint32_t)lf[r].size();
+    const PipeChunks pc = pipe_chunks(rf, nfar, gthreads);
+    const uint32_t clen = pc.clen, nchunk = pc.nchunk;
     uint16_t crow[BS + 1];
     crow[0] = 0;
-    uint32_t nchunk = 0;
-    for (int r = 0; r < BS; ++r) {
-      nchunk += ((uint32_t)lf[r].size() + clen - 1) / clen;
-      crow[r + 1] = (uint16_t)nchunk;
-    }
+    for (int r = 0; r < BS; ++r) crow[r + 1] = (uint16_t)(crow[r] + (rf[r] + clen - 1) / clen);
     if (nchunk > (uint32_t)gthreads) throw Error(RCHOL_ERR_INTERNAL, "pipeline record: more chunks than gatherers");
     maxchunk = std::max<int32_t>(maxchunk, (int32_t)nchunk);
     const PipeLayout L = pipe_layout(nchunk, clen, csz, (uint32_t)vsz);
+    if (L.o_crow != pipe_o_crow(vsz)) throw Error(RCHOL_ERR_INTERNAL, "pipeline record: crow offset");
     const size_t base = P.bytes.size();
     P.bytes.resize(base + L.len, 0);
     unsigned char *p = P.bytes.data() + base;
@@ -1152,7 +1168,16 @@ struct RingPos {
 
 // Block-wide barrier 0 over `n` threads, usable from the different loops of
 // warp-specialised code (each thread of the block arrives once per use).
-__device__ __forceinline__ void cta_barrier(unsigned n) { asm volatile("bar.sync 0, %0;\n" ::"r"(n) : "memory"); }
+// Barrier 0 over n threads, returning the OR of every thread's `p`.
+__device__ __forceinline__ bool cta_barrier_or(unsigned n, bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred a, b;\n setp.ne.u32 a, %1, 0;\n bar.red.or.pred b, 0, %2, a;\n selp.u32 %0, 1, 0, b;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)p), "r"(n)
+      : "memory");
+  return r != 0;
+}
 
 template <int SZ>
 __device__ __forceinline__ void cp_async_small(void *smem, const void *gmem) {
@@ -1235,89 +1260,35 @@ __global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__rest
     cp_async_commit();
   };
   for (int k = 0; k < kW2RhsRing - 1; ++k) fetch_rhs(k);
-  // Block k+1's operands (header, inverse row, row offsets and the lane's
-  // first kW2Pre entries) are loaded while block k is solved; the chain of a
-  // step is then the gathers from the window and the broadcast of t.
-  constexpr int kW2Pre = sizeof(VT) == 4 ? 8 : 4;
-  struct Ops {
-    uint32_t nr, row0, e0, e1, csz, o_tinv;
-    const unsigned char *p;
-    const VT *val;
-    uint32_t c[kW2Pre];
-    VT v[kW2Pre];
-  };
-  auto load_ops = [&](int slot, Ops &o) {
-    const unsigned char *p = ring + (size_t)slot * a.bufbytes;
-    const uint4 h = *reinterpret_cast<const uint4 *>(p);
-    o.p = p;
-    o.nr = h.x;
-    o.row0 = h.y;
-    o.csz = h.w;
-    const W2Layout L = w2_layout(h.z, h.w, sizeof(VT));
-    const uint16_t *eoff = reinterpret_cast<const uint16_t *>(p + L.o_eoff);
-    o.e0 = eoff[lane];
-    o.e1 = eoff[lane + 1];
-    o.val = reinterpret_cast<const VT *>(p + L.o_val);
-    o.o_tinv = (uint32_t)L.o_tinv;
-#pragma unroll
-    for (int u = 0; u < kW2Pre; ++u) {
-      const uint32_t e = o.e0 + u;
-      const bool ok = e < o.e1;
-      o.c[u] = !ok ? 0u
-                   : o.csz == 2 ? (uint32_t)reinterpret_cast<const uint16_t *>(p + L.o_col)[e]
-                                : reinterpret_cast<const uint32_t *>(p + L.o_col)[e];
-      o.v[u] = ok ? o.val[e] : VT(0);
-    }
-  };
-  RingPos pos;  // slot of block k
+  RingPos pos;
   int k = 0;
-  bool ok = __all_sync(0xffffffffu, nb == 0 || mbar_wait(bar + 0, 0u));
-  Ops cur;
-  if (ok && nb > 0) load_ops(0, cur);
-  for (; ok && k < nb; ++k) {
+  bool ok = true;
+  for (; k < nb; ++k) {
     fetch_rhs(k + kW2RhsRing - 1);
-    // the window's values for block k's preloaded entries first (the chain)
-    VT g[kW2Pre];
-#pragma unroll
-    for (int u = 0; u < kW2Pre; ++u) g[u] = xw[cur.c[u] & wmask];
-    VT m[BS];  // block k's inverse row, after the gathers in the load queue
-    load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(cur.p + cur.o_tinv), lane, m);
-    RingPos nxt = pos;
-    nxt.next(NB);
-    Ops nx;
-    const bool more = k + 1 < nb;
-    if (more) {
-      ok = __all_sync(0xffffffffu, mbar_wait(bar + nxt.slot, nxt.par));
-      if (!ok) break;
-      load_ops(nxt.slot, nx);
-    }
-    VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-#pragma unroll
-    for (int u = 0; u < kW2Pre; u += 4) {
-      a0 = fma(cur.v[u], g[u], a0);
-      a1 = fma(cur.v[u + 1], g[u + 1], a1);
-      a2 = fma(cur.v[u + 2], g[u + 2], a2);
-      a3 = fma(cur.v[u + 3], g[u + 3], a3);
-    }
-    VT sum = (a0 + a1) + (a2 + a3);
-    if (cur.e1 > cur.e0 + kW2Pre) {  // the rest of a long row
-      const W2Layout L = w2_layout(0, cur.csz, sizeof(VT));
-      sum += cur.csz == 2
-                 ? run_dot(reinterpret_cast<const uint16_t *>(cur.p + L.o_col), cur.val, xw, wmask, cur.e0 + kW2Pre, cur.e1)
-                 : run_dot(reinterpret_cast<const uint32_t *>(cur.p + L.o_col), cur.val, xw, wmask, cur.e0 + kW2Pre,
-                           cur.e1);
-    }
+    ok = __all_sync(0xffffffffu, mbar_wait(bar + pos.slot, pos.par));
+    if (!ok) break;
     cp_async_wait<kW2RhsRing - 1>();  // block k's right-hand side (this lane's own copy) is in
+    const unsigned char *p = ring + (size_t)pos.slot * a.bufbytes;
+    const uint4 h = *reinterpret_cast<const uint4 *>(p);
+    const uint32_t nr = h.x, row0 = h.y, nent = h.z, csz = h.w;
+    const W2Layout L = w2_layout(nent, csz, sizeof(VT));
+    VT m[BS];
+    load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + L.o_tinv), lane, m);
+    const uint16_t *eoff = reinterpret_cast<const uint16_t *>(p + L.o_eoff);
+    const VT *val = reinterpret_cast<const VT *>(p + L.o_val);
+    const uint32_t e0 = eoff[lane], e1 = eoff[lane + 1];
+    const VT sum = csz == 2 ? run_dot(reinterpret_cast<const uint16_t *>(p + L.o_col), val, xw, wmask, e0, e1)
+                            : run_dot(reinterpret_cast<const uint32_t *>(p + L.o_col), val, xw, wmask, e0, e1);
     const void *rp = rq + (k & (kW2RhsRing - 1)) * BS + lane;
     const VT q0 = a.acc ? *reinterpret_cast<const VT *>(rp) : (VT) * reinterpret_cast<const InT *>(rp);
-    tsh[lane] = lane < (int)cur.nr ? q0 - sum : VT(0);
+    tsh[lane] = lane < (int)nr ? q0 - sum : VT(0);
     __syncwarp();
     const VT x = apply_row(m, tsh);
-    if (lane < (int)cur.nr) {
-      xw[(cur.row0 + lane) & wmask] = x;
-      out[nd.begin + cur.row0 + lane] = (OutT)x;
+    if (lane < (int)nr) {
+      xw[(row0 + lane) & wmask] = x;
+      out[nd.begin + row0 + lane] = (OutT)x;
     }
-    __syncwarp();  // block k's slot and tsh free again
+    __syncwarp();  // slot and tsh free again
     oc.advance(k + NB, lane);  // the lowest record index used below
     if (k + NB < nb) {
       if (lane == 0) fence_proxy_async();
@@ -1327,8 +1298,7 @@ __global__ void __launch_bounds__(256) w2_kernel(W2Args<VT> a, const InT *__rest
       const int64_t o0 = oc.get(k + a.pf), o1 = oc.get(k + a.pf + 1);
       if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
     }
-    pos = nxt;
-    if (more) cur = nx;
+    pos.next(NB);
   }
   if (!ok) {  // give up: wait (bounded) for the copies still in flight, one per slot
     if (lane == 0) {
@@ -1384,7 +1354,6 @@ template <typename VT, typename InT, typename OutT, bool UPPER>
 __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArgs<VT> a, const InT *__restrict__ in,
                                                                          OutT *__restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int abort_flag;
   const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int RING = a.ring, nb = nd.nblocks;
@@ -1400,7 +1369,6 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
   OffCache oc;
   if (warp == 3) oc.init(a.blk_off + nd.blk0, nb, lane);
   if (tid == 0) {
-    abort_flag = 0;
     for (int i = 0; i < RING; ++i) mbar_init(bar + i, 1);
     fence_mbar_init();
   }
@@ -1421,13 +1389,14 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
   }
   __syncthreads();
   auto slot_ptr = [&](int slot) { return ring + (size_t)slot * a.bufbytes; };
-  // warp 3 (the first gatherer warp) streams the records: into every slot
-  // first, then record k into the slot of record k - RING; its lane 0 waits
-  // for record k four steps before use, so that after the next barrier every
-  // warp may read records up to k (each role loads its next step's operands
-  // a step ahead).
+  // warp 3 streams the records: into every slot first, then record k into
+  // the slot of record k - RING (all reads of that slot finished before the
+  // last barrier); its lane 0 waits for record k four steps before use, so
+  // that after the next barrier every warp may read records up to k (each
+  // role loads its next step's operands a step ahead).
   RingPos ld, wt;
   int issued = 0, waited = 0;
+  bool failed = false;  // warp 3 lane 0: a bounded wait gave up
   auto issue = [&](int k) {
     const int64_t o0 = oc.get(k), o1 = oc.get(k + 1);
     if (lane == 0) bulk_load(slot_ptr(ld.slot), a.blocks + o0, (uint32_t)(o1 - o0), bar + ld.slot);
@@ -1437,7 +1406,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
   auto wait_next = [&]() {  // warp 3 lane 0: the next record in order
     if (!mbar_wait(bar + wt.slot, wt.par)) {
       atomicOr(&g_solve_status, 1u);
-      abort_flag = 1;
+      failed = true;
     }
     wt.next(RING);
     ++waited;
@@ -1445,12 +1414,13 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
   if (warp == 3) {
     for (int k = 0; k < RING && k < nb; ++k) issue(k);
     if (lane == 0)
-      while (waited < 4 && waited < nb && !abort_flag) wait_next();
+      while (waited < 4 && waited < nb && !failed) wait_next();
   }
-  __syncthreads();
+  bool stop = __syncthreads_or(failed);
   // Each role runs its own loop over the steps (registers are then allocated
   // per role); every loop passes the same block-wide barrier once per step,
-  // after which abort_flag is read: uniform across the block.
+  // which also ORs the streamer's failure flag into `stop` (uniform across
+  // the block, without a shared-memory read on any role's chain).
   const unsigned nthreads = blockDim.x;
   if (warp == 0) {  // solver: x_s = w_s + y_s - P_s x_{s-1}
     VT pr[BS], xb[BS];
@@ -1459,7 +1429,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     uint32_t s_nr = 0, s_row0 = 0;
     RingPos rp;  // record of the solver's next block
     for (int s = -2; s < nb; ++s) {
-      if (!abort_flag) {
+      if (!stop) {
         if (s >= 0) {
           VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
@@ -1499,7 +1469,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
           }
         }
       }
-      cta_barrier(nthreads);
+      stop = cta_barrier_or(nthreads, failed);
     }
   } else if (warp == 1) {  // reducer: w of block s+1 = T^-1 (acc - chunk sums)
     VT m[BS];                // inverse row of block s+1, loaded in step s-1
@@ -1510,8 +1480,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
       rp.next(RING);
       load_tinv_row<VT, UPPER>(reinterpret_cast<const VT *>(p + 64), lane, mm);
       const uint4 h0 = *reinterpret_cast<const uint4 *>(p);
-      const uint4 h1 = *reinterpret_cast<const uint4 *>(p + 16);
-      const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h1.w);
+      const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + pipe_o_crow(sizeof(VT)));
       nr = h0.x;
       row0 = h0.y;
       a0 = crow[lane];
@@ -1520,7 +1489,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     if (nb > 0) load_next(m, r_nr, r_row0, c0, c1);  // block 0 (records 0..3 are in)
     for (int s = -2; s < nb; ++s) {
       const int bk = s + 1;
-      if (!abort_flag && bk >= 0 && bk < nb) {
+      if (!stop && bk >= 0 && bk < nb) {
         // this step's reads first: shared-memory requests are served in
         // order, so the next block's operands are loaded after them
         const VT far = range_sum(part + (size_t)(bk & 1) * a.maxchunk, c0, c1);
@@ -1529,7 +1498,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
         wbuf[(bk & 1) * BS + lane] = apply_row(m, tb);
         if (bk + 1 < nb) load_next(m, r_nr, r_row0, c0, c1);
       }
-      cta_barrier(nthreads);
+      stop = cta_barrier_or(nthreads, failed);
     }
   } else if (warp == 2) {  // mixer: y of block s+1 = -Q x of block s-1
     VT qr[BS];               // Q's row of block s+1, loaded in step s-1
@@ -1551,7 +1520,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     if (nb > 0) load_next(qr, m_pprow0);
     for (int s = -2; s < nb; ++s) {
       const int bk = s + 1;
-      if (!abort_flag && bk >= 0 && bk < nb) {
+      if (!stop && bk >= 0 && bk < nb) {
         VT y = VT(0);
         if (bk >= 2) {
           VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
@@ -1569,9 +1538,23 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
         ybuf[(bk & 1) * BS + lane] = y;
         if (bk + 1 < nb) load_next(qr, m_pprow0);  // after this step's reads (served in order)
       }
-      cta_barrier(nthreads);
+      stop = cta_barrier_or(nthreads, failed);
     }
-  } else {  // gatherers: far sums of block s+2; warp 3 also streams the records
+  } else if (warp == 3) {  // streams the records
+    for (int s = -2; s < nb; ++s) {
+      if (!stop && s >= 0) {  // record s+RING into the slot of record s (free since the last barrier)
+        const int k = s + RING;
+        oc.advance(a.pf ? min(k, s + a.pf) : k, lane);  // the lowest record index used this step
+        if (k < nb) issue(k);
+        if (a.pf && s + a.pf < nb) {
+          const int64_t o0 = oc.get(s + a.pf), o1 = oc.get(s + a.pf + 1);
+          if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
+        }
+        if (lane == 0 && s + 4 < nb) wait_next();  // record s+4, read from the next step on
+      }
+      stop = cta_barrier_or(nthreads, failed);
+    }
+  } else {  // gatherers: far sums of block s+2
     const int g = tid - 32 * kPipeRoleWarps;
     RingPos rp;
     rp.next(RING);
@@ -1604,20 +1587,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     };
     if (nb > 2) load_next(2);
     for (int s = -2; s < nb; ++s) {
-      if (!abort_flag) {
-        if (warp == 3 && s >= 0) {  // record s+RING into the slot of record s (free since the last barrier)
-          const int k = s + RING;
-          oc.advance(a.pf ? min(k, s + a.pf) : k, lane);  // the lowest record index used this step
-          if (k < nb) {
-            if (lane == 0) fence_proxy_async();
-            issue(k);
-          }
-          if (a.pf && s + a.pf < nb) {
-            const int64_t o0 = oc.get(s + a.pf), o1 = oc.get(s + a.pf + 1);
-            if (lane == 0) prefetch_l2(a.blocks + o0, (uint32_t)(o1 - o0));
-          }
-          if (lane == 0 && s + 4 < nb) wait_next();  // record s+4, read from the next step on
-        }
+      if (!stop) {
         const int bk = s + 2;
         if (bk >= 2 && bk < nb) {
           // this step: the preloaded entries of block bk, the rest from the record
@@ -1646,10 +1616,10 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
           if (bk + 1 < nb) load_next(bk + 1);
         }
       }
-      cta_barrier(nthreads);
+      stop = cta_barrier_or(nthreads, failed);
     }
   }
-  if (abort_flag && warp == 3 && lane == 0) {
+  if (stop && warp == 3 && lane == 0) {
     // copies that may still be in flight: those issued and not waited for (one per slot)
     while (waited < issued) {
       (void)mbar_wait(bar + wt.slot, wt.par);
@@ -1697,7 +1667,7 @@ constexpr int kPipeRingMin = 5;              // pipeline format: records k+1..k+
 // Pipeline team size of a stage with `pieces` pieces: 16 warps where at
 // most one piece runs per SM, fewer (several teams per SM) beyond.
 static int pipe_warps_for(int pieces, int sms, size_t vsz) {
-  return pieces <= sms ? (vsz == 8 ? 12 : 16) : pieces <= 2 * sms ? 8 : 4;
+  return pieces <= sms ? (vsz == 8 ? 12 : 16) : pieces <= 2 * sms ? 8 : 6;
 }
 
 static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<int32_t> &ci,
@@ -1718,9 +1688,9 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   // backward).  The record of the block at processing position q of a piece
   // that starts at position p holds its rows' entries whose columns lie in
   // positions p..q-1 of the node (entries in earlier pieces are external);
-  // rec_bound is an upper bound of its length in the given format, with the
-  // pipeline format's split by distance (1, 2, more) and `gth` gatherer or
-  // helper threads.
+  // rec_bound is an upper bound of its length in the given format (the exact
+  // length for the pipeline format, split by distance 1, 2, more), with
+  // `gth` gatherer or helper threads.
   struct NodeView {
     int64_t b, e, nb;
   };
@@ -1729,9 +1699,8 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     const int64_t r0 = v.b + bq * BS, r1 = std::min(v.e, r0 + BS);
     const size_t csz = v.e - v.b > 65535 ? 4 : 2;
     size_t cnt = 0, far = 0;
-    uint32_t n1 = 0, n2 = 0;
+    uint32_t rf[BS] = {};
     for (int64_t i = r0; i < r1; ++i) {
-      uint32_t m1 = 0, m2 = 0;
       for (int64_t t = rp[i]; t < rp[i + 1]; ++t) {
         const int64_t c = ci[t];
         if (c < v.b || c >= v.e || (c >= r0 && c < r1)) continue;
@@ -1739,15 +1708,14 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
         const int64_t d = upper ? cb - bq : bq - cb;  // blocks back in processing order
         if (d > q - p) continue;                      // in an earlier piece: external
         ++cnt;
-        if (d == 1) ++m1;
-        else if (d == 2) ++m2;
-        else ++far;
+        if (d > 2) {
+          ++far;
+          ++rf[i - r0];
+        }
       }
-      n1 = std::max(n1, m1);
-      n2 = std::max(n2, m2);
     }
     if (fmt == FMT_WARP) return w2_record_bound(cnt, vsz, csz);
-    if (fmt == FMT_PIPE) return pipe_record_bound(far, (size_t)gth, vsz, csz);
+    if (fmt == FMT_PIPE) return pipe_record_len(rf, (uint32_t)far, gth, vsz, csz);
     return team_record_bound(cnt, (size_t)gth, vsz, csz);
   };
   // Cuts a node into pieces of whole blocks whose shared memory fits:
