@@ -202,6 +202,20 @@ int rchol_gpu_trsv_d(rchol_factor_t G, int transpose, const double *d_in, double
 /* y = A x (c++/util/pcg.cpp:130-138); device pointers. */
 int rchol_gpu_spmv_d(rchol_matrix_t A, const double *d_x, double *d_y, int64_t nrhs,
                      void *stream);
+/* Status of the triangular-solve kernels since the last check (no reference
+ * counterpart: the reference's solves are host loops).  Their waits for
+ * record copies are bounded; a wait that gives up marks a device-wide flag
+ * and the kernel finishes without using the data.  This call synchronizes
+ * `stream`, reads and clears the flag, and returns RCHOL_OK or
+ * RCHOL_ERR_TIMEOUT (a wait gave up: the solve's output is not valid).  The
+ * PCG entry points check it before returning; after
+ * rchol_gpu_precond_d / _noalloc_d / rchol_gpu_trsv_d the caller does.  The
+ * flag is shared by all streams of the device. */
+int rchol_gpu_solve_status(void *stream);
+/* Runs one bounded wait that nothing completes (`polls` polls of an mbarrier
+ * no thread arrives at) and returns rchol_gpu_solve_status: RCHOL_ERR_TIMEOUT
+ * shows the timeout path works on this device, without a fault. */
+int rchol_gpu_wait_selftest(uint32_t polls, void *stream);
 
 /* ---- differentiation ---------------------------------------------------------
  * No counterpart in the reference (its Python/MATLAB front ends are not

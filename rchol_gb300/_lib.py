@@ -61,6 +61,8 @@ SIGNATURES = [
     ("rchol_gpu_precond_noalloc_d", C.c_int, [_vp, _vp, _vp, _vp]),
     ("rchol_gpu_trsv_d", C.c_int, [_vp, C.c_int, _vp, _vp, _i64, _vp]),
     ("rchol_gpu_spmv_d", C.c_int, [_vp, _vp, _vp, _i64, _vp]),
+    ("rchol_gpu_solve_status", C.c_int, [_vp]),
+    ("rchol_gpu_wait_selftest", C.c_int, [C.c_uint32, _vp]),
     ("rchol_gpu_edge_grad_d", C.c_int, [_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
 ]
 

@@ -38,6 +38,9 @@ void pcg_batch_device(const rchol_matrix_s &A, const rchol_factor_s &F, int64_t 
                       cudaStream_t s);
 void pcg_batch_host(const rchol_matrix_s &A, const rchol_factor_s &F, int64_t nseg, const int64_t *seg,
                     const double *b, double *x, double tol, int maxit, double *relres, int *itr);
+uint32_t take_solve_status(cudaStream_t s);
+void check_solve_status(cudaStream_t s);
+void wait_selftest(uint32_t polls, cudaStream_t s);
 void edge_grad(int64_t m, const int64_t *ei, const int64_t *ej, const double *lam, const double *x, double *g,
                cudaStream_t s);
 void precond_noalloc(const rchol_factor_s &F, const double *r, double *z, cudaStream_t s);
@@ -339,6 +342,7 @@ int rchol_gpu_pcg_d(rchol_matrix_t A, rchol_factor_t G, const double *d_b, doubl
   RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   RCHOL_CHECK_ARG(maxit >= 0, "maxit must be nonnegative");
   pcg_device(*A, *G, d_b, d_x, (int)nrhs, tol, maxit, relres, itr, as_stream(stream));
+  check_solve_status(as_stream(stream));
   API_END
 }
 
@@ -349,6 +353,7 @@ int rchol_gpu_pcg(rchol_matrix_t A, rchol_factor_t G, const double *b, double *x
   RCHOL_CHECK_ARG(A->n == G->n, "matrix and factor sizes differ");
   RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   pcg_host(*A, *G, b, x, (int)nrhs, tol, maxit, relres, itr);
+  check_solve_status(nullptr);
   API_END
 }
 
@@ -368,6 +373,7 @@ int rchol_gpu_pcg_batch_d(rchol_matrix_t A, rchol_factor_t G, int64_t nsys, cons
   RCHOL_CHECK_ARG(maxit >= 0, "maxit must be nonnegative");
   check_systems(A, nsys, sys_ptr);
   pcg_batch_device(*A, *G, nsys, sys_ptr, d_b, d_x, tol, maxit, relres, itr, as_stream(stream));
+  check_solve_status(as_stream(stream));
   API_END
 }
 
@@ -379,6 +385,7 @@ int rchol_gpu_pcg_batch(rchol_matrix_t A, rchol_factor_t G, int64_t nsys, const 
   RCHOL_CHECK_ARG(maxit >= 0, "maxit must be nonnegative");
   check_systems(A, nsys, sys_ptr);
   pcg_batch_host(*A, *G, nsys, sys_ptr, b, x, tol, maxit, relres, itr);
+  check_solve_status(nullptr);
   API_END
 }
 
@@ -404,6 +411,19 @@ int rchol_gpu_trsv_d(rchol_factor_t G, int transpose, const double *d_in, double
   RCHOL_CHECK_ARG(G && d_in && d_out, "null argument");
   RCHOL_CHECK_ARG(nrhs >= 1 && nrhs <= 256, "nrhs must be in [1, 256]");
   trsv(*G, transpose != 0, d_in, d_out, (int)nrhs, as_stream(stream));
+  API_END
+}
+
+int rchol_gpu_solve_status(void *stream) {
+  API_BEGIN
+  check_solve_status(as_stream(stream));
+  API_END
+}
+
+int rchol_gpu_wait_selftest(uint32_t polls, void *stream) {
+  API_BEGIN
+  wait_selftest(polls, as_stream(stream));
+  check_solve_status(as_stream(stream));
   API_END
 }
 

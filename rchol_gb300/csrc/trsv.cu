@@ -2137,6 +2137,45 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
   }
 }
 
+// ---- status of the bounded waits ------------------------------------------------------------
+
+namespace {
+// One thread waits on an mbarrier that nothing arrives at, for `polls` polls,
+// and records the timeout like the solve kernels do: the path a failed
+// record copy takes, exercised without a fault.
+__global__ void wait_selftest_kernel(uint32_t polls) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  bool done = false;
+  for (uint32_t i = 0; i < polls && !done; ++i) done = mbar_test(&bar, 0);
+  if (!done) atomicOr(&g_solve_status, 1u);
+}
+}  // namespace
+
+uint32_t take_solve_status(cudaStream_t s) {
+  RCHOL_CUDA(cudaStreamSynchronize(s));
+  uint32_t v = 0;
+  RCHOL_CUDA(cudaMemcpyFromSymbol(&v, g_solve_status, sizeof(v)));
+  if (v) {
+    const uint32_t zero = 0;
+    RCHOL_CUDA(cudaMemcpyToSymbol(g_solve_status, &zero, sizeof(zero)));
+  }
+  return v;
+}
+
+void check_solve_status(cudaStream_t s) {
+  const uint32_t v = take_solve_status(s);
+  if (v) throw Error(RCHOL_ERR_TIMEOUT, "a triangular-solve kernel gave up waiting for a record copy");
+}
+
+void wait_selftest(uint32_t polls, cudaStream_t s) {
+  wait_selftest_kernel<<<1, 32, 0, s>>>(polls);
+  note_launch();
+  RCHOL_CUDA(cudaGetLastError());
+}
+
 // ---- autotuning of the launch-time choices -----------------------------------------------
 
 std::pair<double, double> tune_solves(const rchol_factor_s &F, SolvePlan &P, cudaStream_t s) {

@@ -27,6 +27,7 @@ def main(argv=None):
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     p.add_argument("--rhs", type=int, default=1)
     p.add_argument("--reps", type=int, default=1)
+    p.add_argument("--tune", action="store_true", help="tune the solves' launch choices first (Factor.tune)")
     args = p.parse_args(argv)
 
     import torch
@@ -54,6 +55,8 @@ def main(argv=None):
     op = ops[args.op]
     _lib.check(op())  # first call builds the lazily created parts of the plan
     torch.cuda.synchronize()
+    if args.tune:
+        print("tuned:", F.tune())
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
