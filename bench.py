@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--no-extras", action="store_true",
                    help="skip the k-right-hand-side (128^3, k=32), batched-systems (512 2D grids) and "
                         "differentiation (1024^2 adjoint solve) lines")
+    p.add_argument("--config", default="bench", choices=["bench", "c5"],
+                   help="c5: the large high-contrast configuration alone (--n 512: 134M unknowns, checkerboard "
+                        "of 1 and 1e4 in 8^3-cell blocks, k=8, FP32 G), with device and host peak memory")
     return p.parse_args()
 
 
@@ -136,6 +139,45 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+class MemSampler:
+    """Device memory in use (nvidia-smi, every 200 ms) while the block runs."""
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.mib = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=memory.used", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            try:
+                self.mib.append((time.time(), float(line.strip())))
+            except ValueError:
+                pass
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def peak_gb(self, t0=None, t1=None):
+        v = [m for t, m in self.mib if (t0 is None or t >= t0) and (t1 is None or t <= t1)]
+        return round(max(v) * 1048576 / 1e9, 2) if v else None
 
 
 def measured_peak_hbm():
@@ -576,6 +618,96 @@ def differentiation_reference(A, b, xt, w, ei, ej, gw, lam_gpu, rng, samples=200
             "lu_vs_fd": float(np.abs(g_lu - fd).max() / scale)}
 
 
+def run_c5(args, rank, local):
+    """The large high-contrast configuration: 7-point Laplacian on an n^3 grid
+    whose cell coefficients form a checkerboard of 1 and 1e4 in 8^3-cell
+    blocks (Dirichlet boundary), k = 8 right-hand sides N(0,1), FP32 G, block
+    PCG to --tol.  Reports each phase's time, the iterations, the FP64
+    host-recomputed residual of every right-hand side, the device memory in
+    use at its peak (nvidia-smi) against 180 GB, and the host's peak resident
+    memory (this process; the largest forked ordering worker)."""
+    import resource
+
+    import torch
+
+    import rchol_gb300 as R
+    from rchol_gb300 import _lib, generators
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = _lib.lib()
+    k = 8
+    times = {}
+    marks = [("start", time.time())]
+    with MemSampler(local) as mem:
+        time.sleep(1.0)  # samples before any allocation
+        t0 = time.time()
+        A = generators.checkerboard_3d(args.n, block=8, lo=1.0, hi=1e4)
+        n = A.shape[0]
+        times["generate"] = time.time() - t0
+        marks.append(("generate", time.time()))
+        leaves = args.leaves if args.leaves > 0 else max(1, 2048 * (n // (256 ** 3)))  # ~8,200-row subdomains
+        t0 = time.time()
+        tree = R.Tree.build(A.indptr, A.indices, leaves)
+        perm, _ = tree.arrays()
+        times["order"] = time.time() - t0
+        marks.append(("order", time.time()))
+        t0 = time.time()
+        Ad = R.Matrix.create(A.indptr, A.indices, A.data, tree)
+        torch.cuda.synchronize()
+        times["upload"] = time.time() - t0
+        marks.append(("upload", time.time()))
+        t0 = time.time()
+        F = R.Factor.compute(Ad, tree, seed=args.seed, precision=R.PREC_FP32)
+        torch.cuda.synchronize()
+        times["factor_gpu"] = time.time() - t0
+        marks.append(("factor_gpu", time.time()))
+        nnzG = F.nnz
+        g = torch.Generator(device=dev)
+        g.manual_seed(args.seed + 5)
+        B = torch.randn((n, k), generator=g, dtype=torch.float64, device=dev)  # rows in the permuted order
+        X = torch.zeros_like(B)
+        rr = np.zeros(k)
+        it = np.zeros(k, dtype=np.int32)
+        stream = torch.cuda.current_stream(dev)
+
+        def solve():
+            _lib.check(L.rchol_gpu_pcg_d(Ad.ptr, F.ptr, B.data_ptr(), X.data_ptr(), k, args.tol, args.maxit,
+                                         _lib.pd(rr), it.ctypes.data_as(_lib._ip), stream.cuda_stream))
+
+        t0 = time.time()
+        solve()  # first call: captures the iteration graph
+        torch.cuda.synchronize()
+        times["first_solve"] = time.time() - t0
+        marks.append(("first_solve", time.time()))
+        ms = _event_ms(torch, solve, max(1, args.steps), stream)
+        marks.append(("timed_solves", time.time()))
+        time.sleep(0.5)
+    # FP64 host residuals in the caller's order: x(perm) = X, b(perm) = B
+    Xh, Bh = X.cpu().numpy(), B.cpu().numpy()
+    worst = 0.0
+    for j in range(k):
+        x = np.empty(n)
+        b = np.empty(n)
+        x[perm] = Xh[:, j]
+        b[perm] = Bh[:, j]
+        worst = max(worst, float(np.linalg.norm(A @ x - b) / np.linalg.norm(b)))
+    return {
+        "config": "c5",
+        "workload": f"block PCG to {args.tol:g}, k={k}, 7-point Laplacian {args.n}^3 (n={n}, nnz(A)={A.nnz}), "
+                    f"checkerboard of 1 and 1e4 in 8^3-cell blocks, Dirichlet boundary, FP32 G, {leaves} subdomains",
+        "ms_per_solve": round(ms, 1), "unit": "ms", "steps": max(1, args.steps),
+        "iters": [int(it.min()), int(it.max())], "relres_gpu_max": float(rr.max()),
+        "relres_host_fp64_worst": worst, "nnz_G": int(nnzG),
+        "setup_s": {kk: round(v, 2) for kk, v in times.items()},
+        "peak_device_gb": mem.peak_gb(), "device_budget_gb": 180,
+        "peak_device_gb_by_phase": {marks[i][0]: mem.peak_gb(marks[i - 1][1], marks[i][1]) for i in range(1, len(marks))},
+        "device_gb_before_start": mem.peak_gb(marks[0][1] - 1.0, marks[0][1] + 0.9),
+        "peak_host_rss_gb": round(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss * 1024 / 1e9, 2),
+        "peak_host_rss_child_gb": round(resource.getrusage(resource.RUSAGE_CHILDREN).ru_maxrss * 1024 / 1e9, 2),
+    }
+
+
 def cpu_baseline(args, Ap, bp, F64, it64):
     """The oracle restatement of the reference pcg (pinned bit for bit to the
     reference) on the host cores with the GPU's FP64 factor.  Bounded sample:
@@ -709,6 +841,8 @@ def main():
     rank, local, world, pg = dist_init(args)
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.config == "c5":
+        line = run_c5(args, rank, local)
     else:
         line = run_gb300(args, rank, local, world, pg)
     if rank == 0 and line is not None:

@@ -587,10 +587,12 @@ void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t
   for (auto &nd : nodes) maxdepth = std::max(maxdepth, nd.depth);
   std::vector<int> coldepth(next, 1);
   std::vector<char> colleaf(next, 0);
-  for (auto &nd : nodes)
-    for (int64_t c = nd.begin; c < nd.end; ++c) {
-      coldepth[c] = nd.depth;
-      colleaf[c] = nd.leaf;
+  std::vector<int32_t> colnode(next, -1);
+  for (size_t j = 0; j < nodes.size(); ++j)
+    for (int64_t c = nodes[j].begin; c < nodes[j].end; ++c) {
+      coldepth[c] = nodes[j].depth;
+      colleaf[c] = nodes[j].leaf;
+      colnode[c] = (int32_t)j;
     }
   std::vector<int> initdeg(next);
   for (int64_t c = 0; c < next; ++c) initdeg[c] = (int)(ext.rp[c + 1] - ext.rp[c]);
@@ -693,22 +695,32 @@ void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t
     RCHOL_CUDA(cudaStreamSynchronize(s));
     if (hflags[FLAG_FILL] || hflags[FLAG_WIDTH]) {
       // Counts past an overflow are lower bounds (truncated columns sample
-      // less fill), so grow every column of an overflowing depth to twice
-      // the largest count seen there, and overflowing columns to twice theirs.
+      // less fill into the columns after them).  Overflowing columns grow to
+      // twice their count.  In a leaf with an overflow every column grows to
+      // twice its own count (the leaves hold nearly all columns: growing them
+      // all to the leaf depth's largest count took 259 GB at 256^3); the
+      // separator depths, whose columns also receive the leaves' fill, grow
+      // to twice the largest count of their depth.  Runs repeat until
+      // nothing overflows, so the result does not depend on the capacities.
       std::vector<uint32_t> cnt(next);
       fcnt.download(cnt.data(), next, s);
       RCHOL_CUDA(cudaStreamSynchronize(s));
-      std::vector<uint32_t> depth_max(maxdepth + 2, 0);
-      std::vector<char> depth_over(maxdepth + 2, 0);
+      std::vector<uint32_t> depth_max(maxdepth + 1, 0);
+      std::vector<char> depth_over(maxdepth + 1, 0), node_over(nodes.size(), 0);
       for (int64_t c = 0; c < next; ++c) {
-        int dd = colleaf[c] ? maxdepth + 1 : coldepth[c];
-        depth_max[dd] = std::max(depth_max[dd], cnt[c]);
-        if (cnt[c] >= cap[c]) depth_over[dd] = 1;
+        if (cnt[c] < cap[c]) continue;
+        if (colnode[c] >= 0) node_over[colnode[c]] = 1;
+        if (!colleaf[c]) depth_over[coldepth[c]] = 1;
       }
+      for (int64_t c = 0; c < next; ++c)
+        if (!colleaf[c]) depth_max[coldepth[c]] = std::max(depth_max[coldepth[c]], cnt[c]);
       for (int64_t c = 0; c < next; ++c) {
-        int dd = colleaf[c] ? maxdepth + 1 : coldepth[c];
         if (cnt[c] >= cap[c]) cap[c] = std::max<uint32_t>(cap[c] * 2, cnt[c] * 2);
-        if (depth_over[dd]) cap[c] = std::max<uint32_t>(cap[c], depth_max[dd] * 2);
+        if (colleaf[c]) {
+          if (colnode[c] >= 0 && node_over[colnode[c]]) cap[c] = std::max<uint32_t>(cap[c], cnt[c] * 2);
+        } else if (depth_over[coldepth[c]]) {
+          cap[c] = std::max<uint32_t>(cap[c], depth_max[coldepth[c]] * 2);
+        }
       }
       continue;
     }

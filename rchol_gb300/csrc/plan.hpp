@@ -1,6 +1,7 @@
 // Triangular-solve schedule of a factor (built once per factor, see trsv.cu).
 #pragma once
 
+#include <array>
 #include <memory>
 #include <mutex>
 #include <utility>
@@ -49,6 +50,7 @@ struct StreamDir {
   std::vector<int> stage_window;     // warp format: rows of the window of solved values (a power of two)
   std::vector<int> stage_ext;        // 1: the stage has external entries (else it reads the rhs directly)
   std::vector<int> stage_ext_lanes;  // lanes per row of the external sums (1, 4, 8 or 32)
+  std::vector<std::array<int, 9>> stage_smem;  // pipeline / k-team: launch shared memory by ring depth
   DevBuf<int32_t> srows;
   DevBuf<NodeDesc> nodes;
   DevBuf<int64_t> ext_rp;

@@ -386,19 +386,25 @@ __global__ void __launch_bounds__(256) ext_lanes_kernel(const int32_t *__restric
   if (sub == 0) acc[i] = (VT)in[i] - s;
 }
 
+// Status of the solve kernels, read and cleared by the host
+// (take_solve_status): bit 0, a bounded wait gave up; bit 1, a piece did not
+// fit its launch's shared memory.
+__device__ unsigned int g_solve_status;
+
 template <typename VT>
 struct TeamArgs {
   const NodeDesc *nodes;
   int node0;            // first piece of the stage; piece = node0 + blockIdx.x
-  int bufbytes;         // per-record buffer (16-aligned)
-  int ring;             // records in the ring (4..8): the solved block's, the next one's, ring-2 in flight
+  int smem;             // dynamic shared memory of the launch (bytes)
+  int ring;             // most records in the ring (3..8): the solved block's, the next one's, ring-2 in flight
   int maxchunk;         // most chunks of one block (chunk-sum buffer)
   const unsigned char *blocks;
   const int64_t *blk_off;
   const VT *acc;
 };
 
-constexpr int TEAM_RING = 4;  // ring used to cut pieces; launches deepen it where room is left (3 at least)
+constexpr int TEAM_RING = 4;  // ring used to cut pieces; launches deepen it where room is left
+constexpr int TEAM_RING_MIN = 3;
 constexpr int TEAM_RING_MAX = 8;
 
 // cp.async.wait_group takes an immediate: wait until at most n groups pend.
@@ -466,9 +472,17 @@ __global__ void __launch_bounds__(256, 1) team_k_kernel(TeamArgs<VT> a, OutT *ou
   const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ht = tid - 32, TH = (int)blockDim.x - 32, HW = (int)(blockDim.x >> 5) - 1;
-  const int RING = a.ring;
+  // this piece's ring: records of its longest, as many (up to a.ring) as the
+  // launch's shared memory holds besides the chunk sums and its rows
+  const size_t bufbytes = al16((size_t)nd.maxrec);
+  const size_t fixed = 2 * (size_t)BS * KW * sizeof(VT) + (size_t)nd.rows * KW * sizeof(VT);
+  const int RING = min(a.ring, (int)(((size_t)a.smem - min((size_t)a.smem, fixed)) / bufbytes));
+  if (RING < TEAM_RING_MIN) {  // excluded by the plan (every piece fits the smallest ring)
+    if (tid == 0) atomicOr(&g_solve_status, 2u);
+    return;
+  }
   unsigned char *ring = smem;
-  VT *part = reinterpret_cast<VT *>(smem + (size_t)RING * a.bufbytes);  // [2][BS][KW]
+  VT *part = reinterpret_cast<VT *>(smem + (size_t)RING * bufbytes);  // [2][BS][KW]
   VT *xs = part + 2 * BS * KW;                                           // [rows][KW]
   const unsigned char *src = a.blocks;
   const int64_t *boff = a.blk_off + nd.blk0;
@@ -476,7 +490,7 @@ __global__ void __launch_bounds__(256, 1) team_k_kernel(TeamArgs<VT> a, OutT *ou
 
   auto load = [&](int b) {
     if (b < nb) {
-      unsigned char *dst = ring + (size_t)(b % RING) * a.bufbytes;
+      unsigned char *dst = ring + (size_t)(b % RING) * bufbytes;
       const int64_t o0 = boff[b], len = boff[b + 1] - o0;
       for (int64_t o = (int64_t)ht * 16; o < len; o += (int64_t)TH * 16) cp_async16(dst + o, src + o0 + o);
     }
@@ -495,7 +509,7 @@ __global__ void __launch_bounds__(256, 1) team_k_kernel(TeamArgs<VT> a, OutT *ou
 
   for (int b = 0; b < nb; ++b) {
     if (warp == 0) {
-      const unsigned char *p = ring + (size_t)(b % RING) * a.bufbytes;
+      const unsigned char *p = ring + (size_t)(b % RING) * bufbytes;
       const TeamHdr h = read_hdr(p);
       const uint32_t nr = h.nr, row0 = h.row0, prow0 = h.prow0;
       const unsigned char *ncol = p + h.o_ncol;
@@ -529,7 +543,7 @@ __global__ void __launch_bounds__(256, 1) team_k_kernel(TeamArgs<VT> a, OutT *ou
         if (r < (int)nr) xs[(row0 + r) * KW + lane] = t[r];
     } else {
       if (b + 1 < nb) {
-        const unsigned char *p = ring + (size_t)((b + 1) % RING) * a.bufbytes;
+        const unsigned char *p = ring + (size_t)((b + 1) % RING) * bufbytes;
         const TeamHdr h = read_hdr(p);
         const uint32_t csz = h.csz;
         const uint16_t *crow = reinterpret_cast<const uint16_t *>(p + h.o_crow);
@@ -731,6 +745,9 @@ __host__ __device__ constexpr int pq_stride(size_t vsz) { return vsz == 4 ? 36 :
 // byte offset of crow: fixed by the value size
 __host__ __device__ constexpr size_t pipe_o_crow(size_t vsz) { return 64 + vsz * 4 * TQ + 2 * vsz * BS * pq_stride(vsz); }
 constexpr int kPipeRoleWarps = 4;  // solver, reducer, mixer, record streamer; the other warps of a team gather
+constexpr int kPipeRingCut = 6;  // ring the pieces are cut for (launch: up to kPipeRingMax)
+constexpr int kPipeRingMin = 5;  // records k+1..k+3 in use, k+4 waited for, one in flight
+constexpr int kPipeRingMax = 8;
 constexpr int kPipeRowChunks = 8;  // most chunks of one row's far entries
 
 struct PipeLayout {
@@ -927,7 +944,6 @@ void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
 // (bounded) for the ones in flight and finishes without using the data.
 
 constexpr uint32_t kWaitLimit = 1u << 22;
-__device__ unsigned int g_solve_status;  // bit 0: a bounded wait gave up
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -1030,19 +1046,38 @@ __device__ __forceinline__ void load_tinv_row(const VT *tinv, int lane, VT (&m)[
 }
 
 // sum_c m[c] t[c] with t read from shared memory as eight broadcast quads
+// A 32-term dot product in N independent FMA chains (term c in chain c mod
+// N), combined pairwise ((c0 + c1) + (c2 + c3)).  Eight chains for FP64
+// measured slower than four (more registers, no shorter step).
+template <typename VT>
+struct FmaChains {
+  static constexpr int N = 4;
+  VT a[N];
+  __device__ __forceinline__ FmaChains() {
+#pragma unroll
+    for (int i = 0; i < N; ++i) a[i] = VT(0);
+  }
+  __device__ __forceinline__ void add(int c, VT x, VT y) { a[c % N] = fma(x, y, a[c % N]); }
+  __device__ __forceinline__ VT sum() {
+#pragma unroll
+    for (int st = 1; st < N; st *= 2)
+#pragma unroll
+      for (int i = 0; i + st < N; i += 2 * st) a[i] += a[i + st];
+    return a[0];
+  }
+};
+
 template <typename VT>
 __device__ __forceinline__ VT apply_row(const VT (&m)[BS], const VT *tb) {
-  VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  FmaChains<VT> ch;
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     VT t[4];
     ld_quad(tb + 4 * q, t);
-    a0 = fma(m[4 * q + 0], t[0], a0);
-    a1 = fma(m[4 * q + 1], t[1], a1);
-    a2 = fma(m[4 * q + 2], t[2], a2);
-    a3 = fma(m[4 * q + 3], t[3], a3);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) ch.add(4 * q + u, m[4 * q + u], t[u]);
   }
-  return (a0 + a1) + (a2 + a3);
+  return ch.sum();
 }
 
 // Sparse dot products of one lane's row, eight entries at a time: the
@@ -1315,8 +1350,8 @@ template <typename VT>
 struct PipeArgs {
   const NodeDesc *nodes;
   int node0;         // piece = node0 + blockIdx.x
-  int bufbytes;      // bytes of a ring slot (16-aligned)
-  int ring;          // ring slots (5..8): records k+1..k+3 in use, k+4 waited for, the rest in flight
+  int smem;          // dynamic shared memory of the launch (bytes)
+  int ring;          // most ring slots (5..8): records k+1..k+3 in use, k+4 waited for, the rest in flight
   int maxchunk;      // most chunks of one block (chunk-sum buffer)
   int pf;            // records prefetched into L2 ahead of use
   const unsigned char *blocks;
@@ -1330,12 +1365,25 @@ __host__ __device__ constexpr int pipe_max_threads() {
   return sizeof(VT) == 8 ? 384 : 512;
 }
 
-// Shared memory of pipe_kernel besides the record ring: the mbarriers, then
-// the reducer's broadcast buffer t[32], w[2][32], y[2][32], the chunk sums
-// [2][maxchunk], and after the ring the piece's vector padded to whole blocks.
+// Shared memory of pipe_kernel besides the record ring: the mbarriers (room
+// for 8), then the reducer's broadcast buffer t[32], w[2][32], y[2][32], the
+// chunk sums [2][maxchunk], and after the ring the piece's vector padded to
+// whole blocks.
+__host__ __device__ inline size_t pipe_vec_bytes_v(size_t vsz, int maxchunk) {
+  return al16(vsz * (5 * BS + 2 * (size_t)maxchunk));
+}
 template <typename VT>
 __host__ __device__ inline size_t pipe_vec_bytes(int maxchunk) {
-  return al16(sizeof(VT) * (5 * BS + 2 * (size_t)maxchunk));
+  return pipe_vec_bytes_v(sizeof(VT), maxchunk);
+}
+// a pipeline piece's shared memory with a ring of `ring` slots
+inline size_t pipe_piece_smem(size_t vsz, int maxchunk, int rows, int maxrec, int ring) {
+  return al16(8 * 8) + pipe_vec_bytes_v(vsz, maxchunk) + (size_t)((rows + BS - 1) / BS * BS) * vsz +
+         (size_t)ring * al16((size_t)maxrec);
+}
+// a k-team piece's shared memory with a ring of `ring` records
+inline size_t team_piece_smem(size_t vsz, int rows, int maxrec, int ring) {
+  return (size_t)ring * al16((size_t)maxrec) + 2 * (size_t)BS * KW * vsz + (size_t)rows * KW * vsz;
 }
 
 // One thread block per piece.  In step s:
@@ -1356,16 +1404,25 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
   extern __shared__ __align__(16) unsigned char smem[];
   const NodeDesc nd = a.nodes[a.node0 + blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int RING = a.ring, nb = nd.nblocks;
+  const int nb = nd.nblocks;
   const int stride = pq_stride(sizeof(VT));
+  // this piece's ring: slots of its longest record, as many (up to a.ring)
+  // as the launch's shared memory holds besides the vectors and its rows
+  const int rows_pad = (nd.rows + BS - 1) / BS * BS;
+  const size_t slot_bytes = al16((size_t)nd.maxrec);
+  const size_t head = al16(8 * 8) + pipe_vec_bytes<VT>(a.maxchunk) + (size_t)rows_pad * sizeof(VT);
+  const int RING = min(a.ring, (int)(((size_t)a.smem - min((size_t)a.smem, head)) / slot_bytes));
+  if (RING < kPipeRingMin) {  // excluded by the plan (every piece fits the smallest ring)
+    if (tid == 0) atomicOr(&g_solve_status, 2u);
+    return;
+  }
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-  VT *tb = reinterpret_cast<VT *>(smem + al16(8 * (size_t)RING));
+  VT *tb = reinterpret_cast<VT *>(smem + al16(8 * 8));
   VT *wbuf = tb + BS;        // [2][32]
   VT *ybuf = wbuf + 2 * BS;  // [2][32]
   VT *part = ybuf + 2 * BS;  // [2][maxchunk]
   unsigned char *ring = reinterpret_cast<unsigned char *>(tb) + pipe_vec_bytes<VT>(a.maxchunk);
-  VT *xs = reinterpret_cast<VT *>(ring + (size_t)RING * a.bufbytes);
-  const int rows_pad = (nd.rows + BS - 1) / BS * BS;
+  VT *xs = reinterpret_cast<VT *>(ring + (size_t)RING * slot_bytes);
   OffCache oc;
   if (warp == 3) oc.init(a.blk_off + nd.blk0, nb, lane);
   if (tid == 0) {
@@ -1388,7 +1445,7 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     }
   }
   __syncthreads();
-  auto slot_ptr = [&](int slot) { return ring + (size_t)slot * a.bufbytes; };
+  auto slot_ptr = [&](int slot) { return ring + (size_t)slot * slot_bytes; };
   // warp 3 streams the records: into every slot first, then record k into
   // the slot of record k - RING (all reads of that slot finished before the
   // last barrier); its lane 0 waits for record k four steps before use, so
@@ -1431,15 +1488,10 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
     for (int s = -2; s < nb; ++s) {
       if (!stop) {
         if (s >= 0) {
-          VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+          FmaChains<VT> ch;
 #pragma unroll
-          for (int c = 0; c < BS; c += 4) {
-            a0 = fma(pr[c], xb[c], a0);
-            a1 = fma(pr[c + 1], xb[c + 1], a1);
-            a2 = fma(pr[c + 2], xb[c + 2], a2);
-            a3 = fma(pr[c + 3], xb[c + 3], a3);
-          }
-          const VT x = (wbuf[(s & 1) * BS + lane] + ybuf[(s & 1) * BS + lane]) - ((a0 + a1) + (a2 + a3));
+          for (int c = 0; c < BS; ++c) ch.add(c, pr[c], xb[c]);
+          const VT x = (wbuf[(s & 1) * BS + lane] + ybuf[(s & 1) * BS + lane]) - ch.sum();
           if (lane < (int)s_nr) {
             xs[s_row0 + lane] = x;
             out[nd.begin + s_row0 + lane] = (OutT)x;
@@ -1523,17 +1575,15 @@ __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArg
       if (!stop && bk >= 0 && bk < nb) {
         VT y = VT(0);
         if (bk >= 2) {
-          VT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+          FmaChains<VT> ch;
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
             VT xx[4];
             ld_quad(xs + m_pprow0 + 4 * q, xx);
-            a0 = fma(qr[4 * q + 0], xx[0], a0);
-            a1 = fma(qr[4 * q + 1], xx[1], a1);
-            a2 = fma(qr[4 * q + 2], xx[2], a2);
-            a3 = fma(qr[4 * q + 3], xx[3], a3);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) ch.add(4 * q + u, qr[4 * q + u], xx[u]);
           }
-          y = -((a0 + a1) + (a2 + a3));
+          y = -ch.sum();
         }
         ybuf[(bk & 1) * BS + lane] = y;
         if (bk + 1 < nb) load_next(qr, m_pprow0);  // after this step's reads (served in order)
@@ -1661,8 +1711,6 @@ constexpr size_t kSmemCap = 220 * 1024;      // dynamic shared memory a launch m
 constexpr int kW2Ring = 4;                   // warp format: record slots per warp
 constexpr int kW2WindowMax = 8192;           // warp format: most rows in a window
 constexpr size_t kW2WarpBudget = 56 * 1024;  // warp format: shared memory of one warp (at least 4 warps per SM)
-constexpr int kPipeRingCut = 6;              // pipeline format: ring the pieces are cut for (launch: up to 8)
-constexpr int kPipeRingMin = 5;              // pipeline format: records k+1..k+3 in use, k+4 waited for, one in flight
 
 // Pipeline team size of a stage with `pieces` pieces: 16 warps where at
 // most one piece runs per SM, fewer (several teams per SM) beyond.
@@ -1909,6 +1957,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   D.stage_window.clear();
   D.stage_ext.clear();
   D.stage_ext_lanes.clear();
+  D.stage_smem.clear();
   D.stage_row_ptr.assign(1, 0);
   D.steps = 0;
   std::vector<int32_t> srows;
@@ -1927,6 +1976,24 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     }
     const Piece &p0 = pieces[D.stage_ptr[st]];
     const double avg = nrow ? (double)ext / (double)nrow : 0.0;
+    // per ring depth, the launch's shared memory: the largest of its pieces'
+    // (each capped where that piece's deeper ring no longer fits); every
+    // piece must fit the smallest ring
+    std::array<int, 9> sm{};
+    if (p0.fmt != FMT_WARP) {
+      const bool pipe = p0.fmt == FMT_PIPE;
+      const int rmin = pipe ? kPipeRingMin : TEAM_RING_MIN, rmax = pipe ? kPipeRingMax : TEAM_RING_MAX;
+      const int mc = std::max(1, maxchunk);
+      for (int k = D.stage_ptr[st]; k < D.stage_ptr[st + 1]; ++k) {
+        auto need = [&](int r) {
+          return pipe ? pipe_piece_smem(vsz, mc, desc[k].rows, desc[k].maxrec, r)
+                      : team_piece_smem(vsz, desc[k].rows, desc[k].maxrec, r);
+        };
+        if (need(rmin) > kSmemCap) throw Error(RCHOL_ERR_INTERNAL, "solve piece exceeds shared memory");
+        for (int r = rmin; r <= rmax; ++r) sm[r] = std::max<int>(sm[r], (int)std::min(kSmemCap, need(r)));
+      }
+    }
+    D.stage_smem.push_back(sm);
     D.stage_rows.push_back(rows);
     D.stage_maxrec.push_back(maxrec);
     D.stage_fmt.push_back(p0.fmt);
@@ -2118,15 +2185,14 @@ static void launch_streams(const SolvePlan &P, bool upper, const InT *in, OutT *
       a.blocks = D.blocks.p;
       a.blk_off = D.blk_off.p;
       a.acc = src_acc;
-      a.bufbytes = (int)bufbytes;
       a.maxchunk = D.stage_chunks[st];
       a.pf = prefetch_distance(pieces <= sms ? P.knobs.pipe_pf : 0);
       const int warps = D.stage_warps[st];
-      const size_t fixed0 = pipe_vec_bytes<VT>(a.maxchunk) + (size_t)(D.stage_rows[st] + BS - 1) / BS * BS * sizeof(VT);
-      int ring = std::max(kPipeRingMin, std::min(8, P.knobs.pipe_ring));
-      while (ring > kPipeRingMin && al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes > kSmemCap) --ring;
-      a.ring = ring;
-      const size_t bytes = al16(8 * (size_t)ring) + fixed0 + (size_t)ring * bufbytes;
+      // every piece takes the deepest ring up to the knob that fits its own
+      // rows and records; the launch has the largest of their shared memory
+      a.ring = std::max(kPipeRingMin, std::min(kPipeRingMax, P.knobs.pipe_ring));
+      const size_t bytes = (size_t)D.stage_smem[st][a.ring];
+      a.smem = (int)bytes;
       if (bytes > kSmemCap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
       const unsigned threads = 32u * (unsigned)warps;
       if (upper) pipe_kernel<VT, InT, OutT, true><<<pieces, threads, bytes, s>>>(a, in, out);
@@ -2167,7 +2233,8 @@ uint32_t take_solve_status(cudaStream_t s) {
 
 void check_solve_status(cudaStream_t s) {
   const uint32_t v = take_solve_status(s);
-  if (v) throw Error(RCHOL_ERR_TIMEOUT, "a triangular-solve kernel gave up waiting for a record copy");
+  if (v & 1u) throw Error(RCHOL_ERR_TIMEOUT, "a triangular-solve kernel gave up waiting for a record copy");
+  if (v) throw Error(RCHOL_ERR_INTERNAL, "a triangular-solve piece did not fit its launch's shared memory");
 }
 
 void wait_selftest(uint32_t polls, cudaStream_t s) {
@@ -2290,12 +2357,11 @@ static void launch_streams_k(const SolvePlan &P, bool upper, const InT *in, OutT
         D.srows.p + r0, nr, D.ext_rp.p, D.ext_ci.p, ext_v, in, out, acc, k, ld);
     note_launch();
     ta.node0 = D.stage_ptr[st];
-    ta.bufbytes = (int)al16((size_t)D.stage_maxrec[st]);
-    const size_t fixed = 2 * (size_t)BS * KW * sizeof(VT) + (size_t)D.stage_rows[st] * KW * sizeof(VT);
-    int ring = pieces > 2 * sm_count() ? 5 : TEAM_RING_MAX;
-    while (ring > 3 && fixed + (size_t)ring * ta.bufbytes > (size_t)smem_cap) --ring;
-    ta.ring = ring;
-    const size_t bytes = (size_t)ring * ta.bufbytes + fixed;
+    // every piece takes the deepest ring up to this one that fits its own
+    // rows and records; the launch has the largest of their shared memory
+    ta.ring = pieces > 2 * sm_count() ? 5 : TEAM_RING_MAX;
+    const size_t bytes = (size_t)D.stage_smem[st][ta.ring];
+    ta.smem = (int)bytes;
     if (bytes > (size_t)smem_cap) throw Error(RCHOL_ERR_INTERNAL, "triangular-solve piece exceeds shared memory");
     if (upper) team_k_kernel<VT, OutT, true><<<pieces, 256, bytes, s>>>(ta, out, k, ld);
     else team_k_kernel<VT, OutT, false><<<pieces, 256, bytes, s>>>(ta, out, k, ld);
