@@ -696,31 +696,42 @@ void gpu_factor(const HostCsr &ext, const std::vector<TreeNode> &nodes, uint64_t
     if (hflags[FLAG_FILL] || hflags[FLAG_WIDTH]) {
       // Counts past an overflow are lower bounds (truncated columns sample
       // less fill into the columns after them).  Overflowing columns grow to
-      // twice their count.  In a leaf with an overflow every column grows to
-      // twice its own count (the leaves hold nearly all columns: growing them
-      // all to the leaf depth's largest count took 259 GB at 256^3); the
-      // separator depths, whose columns also receive the leaves' fill, grow
-      // to twice the largest count of their depth.  Runs repeat until
+      // twice their count.  The other columns of an overflowing depth grow
+      // to twice the depth's largest count, which settles in one re-run —
+      // unless, for the leaves (nearly all columns), that would not fit in
+      // 30% of the free device memory (the leaf depth's largest count times
+      // 16 million columns took 259 GB at 256^3 on a high-contrast matrix):
+      // then every column of an overflowing leaf grows to twice its own
+      // count, and further re-runs settle the rest.  Runs repeat until
       // nothing overflows, so the result does not depend on the capacities.
       std::vector<uint32_t> cnt(next);
       fcnt.download(cnt.data(), next, s);
       RCHOL_CUDA(cudaStreamSynchronize(s));
-      std::vector<uint32_t> depth_max(maxdepth + 1, 0);
-      std::vector<char> depth_over(maxdepth + 1, 0), node_over(nodes.size(), 0);
+      const int leafd = maxdepth + 1;
+      std::vector<uint32_t> depth_max(maxdepth + 2, 0);
+      std::vector<char> depth_over(maxdepth + 2, 0), node_over(nodes.size(), 0);
       for (int64_t c = 0; c < next; ++c) {
+        const int dd = colleaf[c] ? leafd : coldepth[c];
+        depth_max[dd] = std::max(depth_max[dd], cnt[c]);
         if (cnt[c] < cap[c]) continue;
+        depth_over[dd] = 1;
         if (colnode[c] >= 0) node_over[colnode[c]] = 1;
-        if (!colleaf[c]) depth_over[coldepth[c]] = 1;
       }
-      for (int64_t c = 0; c < next; ++c)
-        if (!colleaf[c]) depth_max[coldepth[c]] = std::max(depth_max[coldepth[c]], cnt[c]);
+      bool leaf_by_depth = true;
+      if (depth_over[leafd]) {
+        uint64_t recs = 0;
+        for (int64_t c = 0; c < next; ++c)
+          if (colleaf[c]) recs += std::max<uint64_t>({cap[c], 2ull * cnt[c], 2ull * depth_max[leafd]});
+        size_t free_b = 0, total_b = 0;
+        RCHOL_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        leaf_by_depth = recs * sizeof(FillRec) <= (uint64_t)(0.3 * (double)free_b);
+      }
       for (int64_t c = 0; c < next; ++c) {
+        const int dd = colleaf[c] ? leafd : coldepth[c];
         if (cnt[c] >= cap[c]) cap[c] = std::max<uint32_t>(cap[c] * 2, cnt[c] * 2);
-        if (colleaf[c]) {
-          if (colnode[c] >= 0 && node_over[colnode[c]]) cap[c] = std::max<uint32_t>(cap[c], cnt[c] * 2);
-        } else if (depth_over[coldepth[c]]) {
-          cap[c] = std::max<uint32_t>(cap[c], depth_max[coldepth[c]] * 2);
-        }
+        if (!depth_over[dd]) continue;
+        if (!colleaf[c] || leaf_by_depth) cap[c] = std::max<uint32_t>(cap[c], depth_max[dd] * 2);
+        else if (colnode[c] >= 0 && node_over[colnode[c]]) cap[c] = std::max<uint32_t>(cap[c], cnt[c] * 2);
       }
       continue;
     }
