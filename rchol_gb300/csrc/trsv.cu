@@ -748,7 +748,10 @@ constexpr int kPipeRoleWarps = 4;  // solver, reducer, mixer, record streamer; t
 constexpr int kPipeRingCut = 6;  // ring the pieces are cut for (launch: up to kPipeRingMax)
 constexpr int kPipeRingMin = 5;  // records k+1..k+3 in use, k+4 waited for, one in flight
 constexpr int kPipeRingMax = 8;
-constexpr int kPipeRowChunks = 8;  // most chunks of one row's far entries
+// most chunks of one row's far entries: FP32 16 (two batches of the
+// reducer's loads, shorter gatherer chunks), FP64 8 (one batch; measured
+// 12% faster than 16 for FP64, 1-3% slower for FP32)
+inline uint32_t pipe_row_chunks(size_t vsz) { return vsz == 4 ? 16u : 8u; }
 
 struct PipeLayout {
   size_t o_tinv, o_p, o_q, o_crow, o_fc, o_fv, len;
@@ -771,17 +774,17 @@ __host__ __device__ inline PipeLayout pipe_layout(uint32_t nchunk, uint32_t clen
 // all): chunks of clen entries (a row's last chunk padded), one chunk per
 // gatherer thread (every row adds at most one partial chunk, so
 // ceil(nfar / (gthreads - 32)) entries per chunk suffice), and no row in more
-// than kPipeRowChunks chunks, so that the reducer's lane for a row sums its
-// chunks in one batch of loads.
+// than pipe_row_chunks(vsz) chunks, so that the reducer's lane for a row sums
+// its chunks in one or two batches of loads.
 struct PipeChunks {
   uint32_t clen, nchunk;
 };
-inline PipeChunks pipe_chunks(const uint32_t *rf, uint32_t nfar, int gthreads) {
-  const uint32_t slots = (uint32_t)std::max(1, gthreads - BS);
+inline PipeChunks pipe_chunks(const uint32_t *rf, uint32_t nfar, int gthreads, size_t vsz) {
+  const uint32_t slots = (uint32_t)std::max(1, gthreads - BS), rc = pipe_row_chunks(vsz);
   uint32_t longest = 0;
   for (int r = 0; r < BS; ++r) longest = std::max(longest, rf[r]);
   PipeChunks c;
-  c.clen = std::max<uint32_t>({1u, (nfar + slots - 1) / slots, (longest + kPipeRowChunks - 1) / kPipeRowChunks});
+  c.clen = std::max<uint32_t>({1u, (nfar + slots - 1) / slots, (longest + rc - 1) / rc});
   c.nchunk = 0;
   for (int r = 0; r < BS; ++r) c.nchunk += (rf[r] + c.clen - 1) / c.clen;
   return c;
@@ -790,7 +793,7 @@ inline PipeChunks pipe_chunks(const uint32_t *rf, uint32_t nfar, int gthreads) {
 // Length of a pipeline record whose rows have `rf[r]` entries more than two
 // blocks back in their piece, for `gthreads` gatherer threads.
 inline size_t pipe_record_len(const uint32_t *rf, uint32_t nfar, int gthreads, size_t vsz, size_t csz) {
-  const PipeChunks c = pipe_chunks(rf, nfar, gthreads);
+  const PipeChunks c = pipe_chunks(rf, nfar, gthreads, vsz);
   return pipe_layout(c.nchunk, c.clen, (uint32_t)csz, (uint32_t)vsz).len;
 }
 
@@ -835,7 +838,7 @@ void build_pipe_piece(const std::vector<int64_t> &rp, const std::vector<int32_t>
     invert_block(T, upper, X);
     uint32_t rf[BS];
     for (int r = 0; r < BS; ++r) rf[r] = (uint32_t)lf[r].size();
-    const PipeChunks pc = pipe_chunks(rf, nfar, gthreads);
+    const PipeChunks pc = pipe_chunks(rf, nfar, gthreads, vsz);
     const uint32_t clen = pc.clen, nchunk = pc.nchunk;
     uint16_t crow[BS + 1];
     crow[0] = 0;
