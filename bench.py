@@ -86,17 +86,16 @@ def max_over_ranks(value, pg, device):
     return float(t.item())
 
 
-class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+class SmiSampler:
+    """One nvidia-smi query on one GPU every 200 ms, in a background thread,
+    while the block runs; `samples` holds (time, fields) pairs."""
 
-    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
-         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+    Q = ""
 
     def __init__(self, gpu_index):
         self.idx = gpu_index
         self.proc = None
-        self.lines = []
+        self.samples = []
 
     def __enter__(self):
         try:
@@ -111,7 +110,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.samples.append((time.time(), [x.strip() for x in line.split(",")]))
 
     def __exit__(self, *a):
         if self.proc:
@@ -121,11 +120,18 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
+
+class ClockSampler(SmiSampler):
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(",")]
+        for _, f in self.samples:
             if len(f) < 7:
                 continue
             try:
@@ -141,42 +147,19 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-class MemSampler:
+class MemSampler(SmiSampler):
     """Device memory in use (nvidia-smi, every 200 ms) while the block runs."""
 
-    def __init__(self, gpu_index):
-        self.idx = gpu_index
-        self.proc = None
-        self.mib = []
-
-    def __enter__(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=memory.used", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
-        except FileNotFoundError:
-            self.proc = None
-        return self
-
-    def _read(self):
-        for line in self.proc.stdout:
-            try:
-                self.mib.append((time.time(), float(line.strip())))
-            except ValueError:
-                pass
-
-    def __exit__(self, *a):
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
+    Q = "memory.used"
 
     def peak_gb(self, t0=None, t1=None):
-        v = [m for t, m in self.mib if (t0 is None or t >= t0) and (t1 is None or t <= t1)]
+        v = []
+        for t, f in self.samples:
+            if (t0 is None or t >= t0) and (t1 is None or t <= t1):
+                try:
+                    v.append(float(f[0]))
+                except (ValueError, IndexError):
+                    pass
         return round(max(v) * 1048576 / 1e9, 2) if v else None
 
 
