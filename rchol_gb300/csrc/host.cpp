@@ -7,8 +7,10 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <future>
 #include <numeric>
 #include <set>
@@ -36,19 +38,43 @@ int host_threads() {
   return h ? (int)std::min(h, 64u) : 4;
 }
 
+// Blocks of at least `grain` indices (and about 16 per thread) handed out in
+// order to the threads as they come free, so that uneven work (large and
+// small pieces of a solve plan) spreads over all threads.  The first
+// exception thrown by any block is rethrown to the caller after all threads
+// have stopped taking blocks.
 void parallel_for(int64_t n, const std::function<void(int64_t, int64_t)> &body, int64_t grain) {
-  int T = host_threads();
+  const int T = host_threads();
   if (n <= grain || T <= 1) {
     body(0, n);
     return;
   }
-  int64_t chunks = std::min<int64_t>(T, (n + grain - 1) / grain);
+  const int64_t block = std::max<int64_t>(std::max<int64_t>(grain, 1), (n + 16 * (int64_t)T - 1) / (16 * (int64_t)T));
+  const int64_t nblocks = (n + block - 1) / block;
+  std::atomic<int64_t> next{0};
+  std::atomic<bool> failed{false};
+  std::exception_ptr first;
+  std::mutex mu;
+  auto worker = [&]() {
+    for (;;) {
+      const int64_t b = next.fetch_add(1);
+      if (b >= nblocks || failed.load()) return;
+      try {
+        body(b * block, std::min(n, (b + 1) * block));
+      } catch (...) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!first) first = std::current_exception();
+        failed.store(true);
+        return;
+      }
+    }
+  };
   std::vector<std::thread> th;
-  for (int64_t c = 0; c < chunks; ++c) {
-    int64_t a = n * c / chunks, b = n * (c + 1) / chunks;
-    th.emplace_back([&body, a, b]() { body(a, b); });
-  }
+  const int64_t nt = std::min<int64_t>(T, nblocks);
+  for (int64_t t = 1; t < nt; ++t) th.emplace_back(worker);
+  worker();
   for (auto &t : th) t.join();
+  if (first) std::rethrow_exception(first);
 }
 
 namespace {

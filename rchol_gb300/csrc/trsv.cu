@@ -1910,11 +1910,16 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
         }
     }
   }, 1 << 14);
-  // block records
+  // block records, the largest pieces first (they take the longest)
   std::vector<PieceBuild> built(np);
   std::vector<int32_t> chunks(np, 0);
+  std::vector<int> by_size(np);
+  for (int k = 0; k < np; ++k) by_size[k] = k;
+  std::stable_sort(by_size.begin(), by_size.end(),
+                   [&](int x, int y) { return pieces[x].e - pieces[x].b > pieces[y].e - pieces[y].b; });
   parallel_for(np, [&](int64_t k0, int64_t k1) {
-    for (int64_t k = k0; k < k1; ++k) {
+    for (int64_t kk = k0; kk < k1; ++kk) {
+      const int k = by_size[kk];
       const Piece &pc = pieces[k];
       if (pc.fmt == FMT_WARP) {
         int64_t reach = 0;
@@ -1945,10 +1950,11 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     total += (int64_t)built[k].bytes.size();
     D.sparse_nnz += built[k].sparse;
   }
-  std::vector<unsigned char> all(total);
+  // every byte is written by one piece's copy: no zero fill
+  std::unique_ptr<unsigned char[]> all(new unsigned char[std::max<int64_t>(total, 1)]);
   parallel_for(np, [&](int64_t k0, int64_t k1) {
     for (int64_t k = k0; k < k1; ++k)
-      std::memcpy(all.data() + blk_off[desc[k].blk0], built[k].bytes.data(), built[k].bytes.size());
+      std::memcpy(all.get() + blk_off[desc[k].blk0], built[k].bytes.data(), built[k].bytes.size());
   }, 1);
   built.clear();
   // stages
@@ -2011,7 +2017,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   D.nblocks = (int64_t)blk_off.size() - np;
   D.ext_nnz = next;
   if (host_copy) {
-    host_copy->blocks.swap(all);
+    host_copy->blocks.assign(all.get(), all.get() + total);
     host_copy->blk_off = blk_off;
     host_copy->desc = desc;
     host_copy->ext_rp = ext_rp;
@@ -2022,7 +2028,7 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
     host_copy->stage_window = D.stage_window;
     return;
   }
-  D.blocks.upload(all.data(), all.size(), s);
+  D.blocks.upload(all.get(), (size_t)total, s);
   D.blk_off.upload(blk_off.data(), blk_off.size(), s);
   D.nodes.upload(desc.data(), np, s);
   D.ext_rp.upload(ext_rp.data(), n + 1, s);
@@ -2031,7 +2037,9 @@ static void build_dir_streams(const std::vector<int64_t> &rp, const std::vector<
   std::vector<float> ev32;
   if (fp32) {
     ev32.resize(next);
-    for (int64_t q = 0; q < next; ++q) ev32[q] = (float)ev[q];
+    parallel_for(next, [&](int64_t q0, int64_t q1) {
+      for (int64_t q = q0; q < q1; ++q) ev32[q] = (float)ev[q];
+    }, 1 << 20);
     D.ext_v32.upload(ev32.data(), next, s);
   }
   D.srows.upload(srows.data(), srows.size(), s);
