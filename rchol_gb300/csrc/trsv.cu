@@ -1395,12 +1395,14 @@ inline size_t team_piece_smem(size_t vsz, int rows, int maxrec, int ring) {
 //                     eight broadcast quads and P_{s+1}'s row;
 //   warp 1 (reducer)  w_{s+1} = T^-1 (acc - chunk sums) of block s+1, then
 //                     the inverse row of block s+2;
-//   warp 2 (mixer)    y_{s+1} = -Q_{s+1} x_{s-1}; streams record s+RING into
-//                     the slot of record s and, one thread, waits for record
-//                     s+3 (the barrier then publishes it to every warp);
-//   warps 3..         far chunk sums of block s+2.
-// One __syncthreads per step.  The piece's right-hand side, then its
-// solution, live in shared memory (xs).
+//   warp 2 (mixer)    y_{s+1} = -Q_{s+1} x_{s-1}, then Q's row of block s+2;
+//   warp 3 (streamer) copies record s+RING into the slot of record s and,
+//                     one thread, waits for record s+4 (the next barrier then
+//                     publishes it to every warp);
+//   warps 4..         far chunk sums of block s+2.
+// One block-wide barrier per step (bar.red.or, carrying the streamer's
+// failure flag).  The piece's right-hand side, then its solution, live in
+// shared memory (xs).
 template <typename VT, typename InT, typename OutT, bool UPPER>
 __global__ void __launch_bounds__(pipe_max_threads<VT>(), 1) pipe_kernel(PipeArgs<VT> a, const InT *__restrict__ in,
                                                                          OutT *__restrict__ out) {
